@@ -1,0 +1,370 @@
+"""Benchmark of the GB300 nearest-neighbour render path (one JSON line).
+
+Workload (the batched configuration): one 128^3 = 2,097,152-point jittered
+coronal-loop snapshot x 64 views (l uniform in [0, 90 deg], b uniform in
+[-20, 20 deg], seeded) x 4 spectral lines (G(T) peaks at logT 5.8/6.0/6.2/6.4,
+lambda0 171/193/211/284 A), 256x256 pixels, 64 lambda bins over a common
++-175 km/s window, 512 LOS samples; one persistent launch captured in a CUDA
+graph.  A step renders the whole batch.  Synthetic data (the reference has no
+benchmark dataset).
+
+value      : line-samples/s of the batched render, inputs resident in HBM, L2
+             flushed (256 MiB write) before each timed step, CUDA events.
+plain_*    : the plain single-request GPU render (512x512, 128 bins, 512
+             samples, l in {0, 30, 60 deg}, b = 0), one request per call --
+             the denominator of the batched-vs-plain metric.
+e2e        : the same batch through the C ABI with pinned host buffers: upload
+             the snapshot, build the index, emissivity, render, download every
+             cube, per step.
+roofline   : the march kernel's algorithmic bytes / its event-timed duration
+             against the measured HBM copy bandwidth.
+cpu_baseline: the oracle (C restatement, OpenMP on all host cores) on a bounded
+             sample of rows of the plain configuration.
+
+--impl reference runs the reference's CPU algorithm (the oracle port; the
+reference's own build needs Boost/GSL, absent on the GPU host) on a bounded
+sample of the batched workload and prints the same metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LOS samples/s batched vs plain GPU at ≤1e-4 rel err; p50/p99 render latency"
+LINES = ((5.8, 171.073, "fe_9"), (6.0, 193.509, "fe_12"), (6.2, 211.317, "fe_14"), (6.4, 284.163, "fe_15"))
+WIDTH = 0.6 * 2.99792458e8 / 171.073  # +-0.3 A at 171 A, in m/s (same velocity window for every line)
+NVIEWS, NX, NY, NZ, NL = 64, 256, 256, 512, 64
+
+
+def _rank_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(seed=1):
+    from fomo_gb300 import synth
+    snap = synth.loop_snapshot(128, seed=seed)
+    tables = [synth.line_table(peak_logT=p, lambda0=lam, ion=ion) for p, lam, ion in LINES]
+    rng = np.random.default_rng(3)
+    ls = rng.uniform(0.0, math.pi / 2, NVIEWS)
+    bs = rng.uniform(-math.pi / 9, math.pi / 9, NVIEWS)
+    return snap, tables, ls, bs
+
+
+def algorithmic_bytes_per_sample(nlines, L, nz):
+    # winning point's FP32 position (12 B) + v_los (4 B) + (eps, w) per line (8 B)
+    # + the output cube written once per ray, spread over its LOS samples
+    return 12 + 4 + 8 * nlines + 4.0 * L * nlines / nz
+
+
+def cpu_baseline_sample(target_s=10.0):
+    """Oracle (C restatement, OpenMP, all host cores) on rows of the plain configuration."""
+    import oracle
+    from fomo_gb300 import synth
+    snap = synth.loop_snapshot(128, seed=1)
+    t = synth.line_table()
+    cores = os.cpu_count() or 1
+    eps, w = oracle.emission(snap, t)
+    nx = ny = 512
+    nz, L = 512, 128
+    width = 0.6 * 2.99792458e8 / t.lambda0
+    rows = 1
+    t0 = time.perf_counter()
+    oracle.nn_render(snap, eps, w, t.lambda0, 0.0, 0.0, nx, ny, nz, L, width, nthreads=cores, rows=(256, 256 + rows))
+    dt = time.perf_counter() - t0
+    rows = int(max(1, min(ny // 2, target_s / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    oracle.nn_render(snap, eps, w, t.lambda0, 0.0, 0.0, nx, ny, nz, L, width, nthreads=cores,
+                     rows=(256 - rows // 2, 256 - rows // 2 + rows))
+    dt = time.perf_counter() - t0
+    samples = rows * nx * nz
+    return {"value": samples / dt, "unit": "LOS samples/s", "cores": cores, "kind": "port",
+            "sample": f"{rows} image rows x 512 rays x 512 samples of the plain 512x512x128 render "
+                      f"(2,097,152 points, l=b=0) by the oracle, {dt:.1f} s"}
+
+
+def run_reference(args):
+    """Reference CPU algorithm (oracle port) on a bounded sample of the batched workload."""
+    import oracle
+    rank, world, _ = _rank_env()
+    if world > 1 and rank != 0:
+        return
+    snap, tables, ls, bs = make_workload()
+    cores = os.cpu_count() or 1
+    payload = [oracle.emission(snap, t) for t in tables]
+    rows = 2
+    times = []
+    for step in range(args.warmup + args.steps):
+        v = step % NVIEWS
+        t0 = time.perf_counter()
+        for (eps, w), t in zip(payload, tables):
+            oracle.nn_render(snap, eps, w, t.lambda0, ls[v], bs[v], NX, NY, NZ, NL, WIDTH, nthreads=cores,
+                             rows=(NY // 2 - rows // 2, NY // 2 - rows // 2 + rows))
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    line_samples = rows * NX * NZ * len(tables)
+    value = line_samples * len(times) / sum(times)
+    ms = 1e3 * sum(times) / len(times)
+    sample = (f"{rows} central rows x {NX} rays x {NZ} samples x {len(tables)} lines of one view per step "
+              f"(oracle, FP64, OpenMP {cores} threads)")
+    out = {"metric": METRIC, "value": value, "unit": "line-samples/s", "impl": "reference", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "batched NN render: 2,097,152-point loop x 64 views x 4 lines, 256x256, "
+                                  "64 bins, 512 LOS samples", "sample_per_step": sample},
+           "cpu_baseline": {"value": value, "unit": "line-samples/s", "cores": cores, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "line-samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+
+    import fomo_gb300 as fg
+
+    rank, world, local = _rank_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    snap, tables, ls, bs = make_workload(seed=1 + rank)
+    ctx = fg.Context(local)
+    sid = ctx.snapshot(snap)
+    tids = [ctx.table(t) for t in tables]
+    reqs = [ctx.request(sid, tid, fg.METHOD_NN, NX, NY, NZ, NL, float(ls[v]), float(bs[v]), WIDTH)
+            for v in range(NVIEWS) for tid in tids]
+    outs = [torch.empty((NY, NX, NL), dtype=torch.float32, device=dev) for _ in reqs]
+    ptrs = [o.data_ptr() for o in outs]
+    stream = torch.cuda.current_stream(dev)
+    sh = ctypes_stream(stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    cache = os.path.join(ROOT, "profiles", "autotune_cache.txt")
+    ctx.autotune(reqs, cache_path=cache if os.path.exists(cache) else None)
+
+    for _ in range(args.warmup):
+        ctx.render_batch_device(reqs, ptrs, stream=sh, graph=True)
+    torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    march_ms = []
+    with Clocks(local) as clk:
+        torch.cuda.synchronize(dev)
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            ctx.render_batch_device(reqs, ptrs, stream=sh, graph=True)
+            ev[k][1].record(stream)
+            march_ms.append(ctx.last_march_ms())
+        torch.cuda.synchronize(dev)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1e3
+    if dist:
+        tt = torch.tensor([t_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+        dist.barrier()
+    line_samples = float(NVIEWS * len(tables) * NX * NY * NZ)
+    value = world * line_samples * args.steps / t_total
+
+    # ---- plain single-request GPU render (denominator)
+    from fomo_gb300 import synth
+    t171 = ctx.table(synth.line_table())
+    preqs = [ctx.request(sid, t171, fg.METHOD_NN, 512, 512, 512, 128, math.radians(a), 0.0, WIDTH)
+             for a in (0.0, 30.0, 60.0)]
+    pout = torch.empty((512, 512, 128), dtype=torch.float32, device=dev)
+    for q in preqs:
+        ctx.render_device(q, pout.data_ptr(), stream=sh)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.fill_(1)
+    e0.record(stream)
+    for q in preqs:
+        ctx.render_device(q, pout.data_ptr(), stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_s = e0.elapsed_time(e1) / 1e3
+    plain_value = 3 * 512 * 512 * 512 / plain_s
+
+    # ---- end to end through the C ABI with pinned host buffers
+    hsnap = [torch.from_numpy(a).pin_memory() for a in snap.arrays()]
+    hout = [torch.empty((NY, NX, NL), dtype=torch.float32).pin_memory() for _ in range(len(reqs))]
+    from fomo_gb300 import Context
+    e2e_times = []
+    h2d = sum(a.numel() * 4 for a in hsnap) + sum(t.G.nbytes + t.logT.nbytes + t.logn.nbytes for t in tables)
+    d2h = sum(o.numel() * 4 for o in hout)
+    e2e_steps = max(1, min(args.steps, 3))
+    for k in range(e2e_steps + 1):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        s2 = ctx_snapshot_from_pinned(ctx, hsnap)
+        tids2 = [ctx.table(t) for t in tables]
+        reqs2 = [ctx.request(s2, tid, fg.METHOD_NN, NX, NY, NZ, NL, float(ls[v]), float(bs[v]), WIDTH)
+                 for v in range(NVIEWS) for tid in tids2]
+        cubes, _ = ctx.render_batch(reqs2, outs=[h.numpy() for h in hout])
+        dt = time.perf_counter() - t0
+        ctx.drop_snapshot(s2)
+        for t in tids2:
+            ctx.drop_table(t)
+        if k > 0:
+            e2e_times.append(dt)
+    e2e_value = world * line_samples * len(e2e_times) / sum(e2e_times)
+
+    # ---- roofline of the march kernel
+    avg_march_s = float(np.mean(march_ms)) / 1e3
+    bps = algorithmic_bytes_per_sample(len(tables), NL, NZ)
+    samples_per_launch = NVIEWS * NX * NY * NZ
+    achieved = bps * samples_per_launch / avg_march_s / 1e9
+    peak, peak_kind = _peaks()
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "march_traffic.json")
+    if os.path.exists(tf):
+        try:
+            with open(tf) as f:
+                traffic = json.load(f).get("bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+
+    if rank == 0:
+        cpu = cpu_baseline_sample() if not args.no_cpu else None
+        out = {
+            "metric": METRIC, "value": value, "unit": "line-samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "batched NN render: 2,097,152-point loop x 64 views x 4 lines, 256x256 px, "
+                                   "64 lambda bins, 512 LOS samples, one persistent launch in a CUDA graph",
+                       "l2": "flushed (256 MiB write) before each timed step; snapshot+payload ~130 MB",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "plain": "512x512 px, 128 bins, 512 samples, l in {0,30,60} deg, b=0, one request per call"},
+            "los_samples_per_step": NVIEWS * NX * NY * NZ,
+            "plain_value": plain_value, "plain_unit": "LOS samples/s",
+            "batched_vs_plain": value / plain_value,
+            "march_ms": float(np.mean(march_ms)),
+            "e2e": {"value": e2e_value, "unit": "line-samples/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": len(e2e_times),
+                    "ms_per_step": 1e3 * float(np.mean(e2e_times))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                         "bytes_per_sample": bps, "kernel": "march_spectral<4,2>"},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": 4 * args.steps,
+        }
+        print(json.dumps(out))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def ctypes_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def ctx_snapshot_from_pinned(ctx, hsnap):
+    import ctypes
+
+    import fomo_gb300 as fg
+    sid = ctypes.c_int()
+    ptrs = [ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float)) for t in hsnap]
+    ctx._check(ctx._L.fomo_snapshot_create(ctx.h, hsnap[0].numel(), *ptrs, ctypes.byref(sid)))
+    return sid.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

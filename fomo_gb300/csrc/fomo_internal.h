@@ -1,0 +1,135 @@
+// Internal structures shared by the CUDA kernels and the host runtime of
+// libfomo_gpu.  Nothing here is part of the public C ABI (include/fomo_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fomo_consts.h"
+
+namespace fomo {
+
+// ---------------------------------------------------------------------------
+// Snapshot: the point cloud, sorted into a uniform grid (cell-major, x fastest)
+// ---------------------------------------------------------------------------
+struct GridParams {
+  float ox, oy, oz;     // grid origin = AABB minimum of the points
+  float h, inv_h;       // cell edge (Mm) and its FP32 reciprocal used for binning
+  int dx, dy, dz;       // cells per axis
+  float minx, miny, minz, maxx, maxy, maxz;  // exact AABB of the points (FP32)
+};
+
+struct SnapDev {
+  int64_t n;
+  const float4* pts;    // sorted: x, y, z (FP32 Mm), original index (int bits)
+  const float4* vel;    // sorted: vx, vy, vz (m/s), 0
+  const int* cell_start;  // dx*dy*dz + 1 slots
+  GridParams g;
+};
+
+// ---------------------------------------------------------------------------
+// One view (l, b) of one snapshot.  Host fills the first block (trig values
+// come from the host libm, as in the reference); the device fills the rest.
+// ---------------------------------------------------------------------------
+enum Method : int { kMethodNN = 0, kMethodThomson = 1 };
+
+struct ViewDesc {
+  // ---- host-filled
+  double cb, sb, cl, sl;     // derotation cos/sin (unclamped)
+  double rcb, rsb;           // rotation used for the extents (Thomson clamps)
+  double blend;              // Thomson pole blend (fomo-thomson.cpp:176), 0 for NN
+  double mdblend;            // Thomson maxdistance blend (fomo-thomson.cpp:249)
+  double lambda_width;       // m/s
+  double lambda0;            // table lambda0 of the primary line (Angstrom)
+  int nx, ny, nz, L;
+  int method;
+  int is_dn;
+  int ray_tile_w, ray_tile_h;  // ray tile shape for the march work order
+  // ---- device-filled by the extents + finalize kernels
+  unsigned long long ext_bits[6];  // order-preserving encodings for atomic min/max
+  double minx, maxx, miny, maxy, minz, maxz;
+  double md;                 // maxdistance
+  double deltaz;
+  double pathlength;
+  double apix;               // DN pixel area (nn:261-262); applied to lines with a DN unit
+  double scale;              // pathlength * 1e8            (non-DN lines)
+  double scale_dn;           // pathlength * 1e8 * apix     (DN lines)
+  double lwa;                // lambda_width in Angstrom (primary line)
+  double dxr, dyr;           // (maxx-minx), (maxy-miny) as the reference evaluates them
+  double* xt;                // nx ray x positions j/(nx-1)*(maxx-minx)+minx (device, filled by finalize)
+  double* yt;                // ny ray y positions
+  float ux, uy, uz;          // LOS unit vector in FP32 for the Doppler term
+  int pad0;
+};
+
+// One spectral line (or broadband channel) rendered with a view.
+struct LineDesc {
+  const float2* ew;          // sorted per-point (eps, fwhm)
+  float* out;                // device cube, (ny*nx*L) floats, L fastest
+  const float* lam;          // L relative wavelengths lambdaval (nn:200), FP64 on host -> FP32
+  double lambda0;
+  double lwa;                // lambda_width * lambda0 / c (Angstrom)
+  float shift_k;             // lambda0 / c in FP32 (Doppler shift per m/s)
+  int is_dn;                 // unit contains "DN": per-pixel scaling
+};
+
+struct MarchArgs {
+  SnapDev snap;
+  ViewDesc* views;           // nviews
+  const int64_t* ray_offset; // nviews + 1, prefix sums of work items per view
+  const LineDesc* lines;     // nviews * nlines
+  int nviews;
+  int nlines;
+  int64_t total_items;
+  unsigned long long* counter;   // work-queue head, zeroed before the launch
+  int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
+  const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
+  const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
+  unsigned int* err;             // device error word (bounds-check builds)
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (defined in the .cu files)
+// ---------------------------------------------------------------------------
+// index.cu
+cudaError_t launch_aabb(const float* x, const float* y, const float* z, int64_t n, unsigned int* bits6,
+                        cudaStream_t s);
+cudaError_t launch_bin_points(const float* x, const float* y, const float* z, int64_t n, GridParams g,
+                              int* cell_of, int* counts, cudaStream_t s);
+cudaError_t launch_exclusive_scan(const int* in, int* out, int64_t count, int* scratch, int64_t scratch_ints,
+                                  cudaStream_t s);
+int64_t exclusive_scan_scratch_ints(int64_t count);
+cudaError_t launch_scatter(const float* x, const float* y, const float* z, const float* vx, const float* vy,
+                           const float* vz, const float* ne, const float* T, int64_t n, const int* cell_of,
+                           const int* cell_start, int* fill, float4* pts, float4* vel, float* ne_s, float* T_s,
+                           cudaStream_t s);
+cudaError_t launch_sort_cells(const int* cell_start, int64_t ncells, float4* pts, float4* vel, float* ne_s,
+                              float* T_s, cudaStream_t s);
+
+// emission.cu
+struct TableDev {
+  int nt, nrho;
+  const float* logT;   // nt
+  const float* logn;   // nrho
+  const float* G;      // nrho * nt
+  double cw;           // linefwhm constant (fomo-CHIANTI.cpp:224)
+  double k;            // normaliseconst * abundratio
+  int imaging;
+};
+cudaError_t launch_emission(const float* ne_s, const float* T_s, int64_t n, TableDev t, float2* ew, cudaStream_t s);
+cudaError_t launch_thomson_emission(const float4* pts, const float* ne_s, int64_t n, float2* totpol,
+                                    cudaStream_t s);
+cudaError_t launch_unsort_payload(const float4* pts, const float2* ew, int64_t n, float* a, float* b,
+                                  cudaStream_t s);
+
+// view.cu
+cudaError_t launch_view_init(ViewDesc* views, int nviews, cudaStream_t s);
+cudaError_t launch_view_extents(SnapDev snap, ViewDesc* views, int nviews, float* s2, cudaStream_t s);
+cudaError_t launch_view_finalize(ViewDesc* views, int nviews, double3* ktab, int ktab_stride, cudaStream_t s);
+
+// march.cu
+cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_L, int sm_count,
+                         cudaStream_t s, int blocks_per_sm_hint);
+int march_bins_per_lane(int nlines, int L);
+
+}  // namespace fomo

@@ -1,0 +1,165 @@
+// Host-side state of a libfomo_gpu context (opaque behind fomo_ctx* in the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/fomo_gpu.h"
+#include "fomo_internal.h"
+
+namespace fomo {
+
+struct TableHost {
+  std::string ion, unit;
+  double lambda0 = 0, atweight = 0;
+  int nt = 0, nrho = 0;
+  bool is_dn = false;
+  std::vector<float> logT, logn, G;
+};
+
+struct TableRec {
+  TableHost h;
+  float* d = nullptr;  // logT | logn | G
+};
+
+struct SnapRec {
+  int64_t n = 0;
+  int64_t ncells = 0;
+  GridParams g{};
+  void* block = nullptr;  // one allocation for everything below
+  size_t bytes = 0;
+  float4* pts = nullptr;
+  float4* vel = nullptr;
+  float* ne = nullptr;
+  float* T = nullptr;
+  int* cell_start = nullptr;
+  float2* totpol = nullptr;  // Thomson payload, built on first use
+};
+
+// Grow-only device scratch; contents belong to the work last enqueued.
+struct Arena {
+  char* base = nullptr;
+  size_t cap = 0;
+  int reserve(fomo_ctx* ctx, size_t bytes);
+};
+
+// Pinned host staging for descriptor uploads; copy_done marks when the last
+// upload from it has executed, before it may be rewritten.
+struct Staging {
+  char* base = nullptr;
+  size_t cap = 0;
+  cudaEvent_t copy_done = nullptr;
+  int reserve(fomo_ctx* ctx, size_t bytes);
+};
+
+// Scratch for one in-flight batch: device arena, pinned descriptor staging and
+// march timing events.  The context has one; the server one per slot.
+struct ScratchSet {
+  Arena arena;
+  Staging staging;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaError_t init() {
+    cudaError_t e = cudaEventCreate(&ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev1);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&staging.copy_done, cudaEventDisableTiming);
+    return e;
+  }
+  void release() {
+    if (staging.copy_done) cudaEventSynchronize(staging.copy_done);
+    if (staging.base) cudaFreeHost(staging.base);
+    staging.base = nullptr;
+    staging.cap = 0;
+    if (staging.copy_done) cudaEventDestroy(staging.copy_done);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    staging.copy_done = ev0 = ev1 = nullptr;
+  }
+};
+
+// One launch of a planned batch: requests sharing (snapshot, method, imaging).
+struct PlanGroup {
+  int snapshot = 0, method = 0, imaging = 0;
+  std::vector<int> reqs;
+  std::vector<std::vector<int>> vreqs;  // requests (lines) of each view
+  int nv = 0, nl = 1, maxL = 1, maxnz = 1, maxnx = 2, maxny = 2;
+  int tw = 8, th = 4, bps = 0;
+  std::vector<const float2*> ew;       // payload per request (NN)
+  const float2* totpol = nullptr;      // Thomson payload
+  bool any_nn = false;
+  int64_t total_items = 0;
+  int vbase = 0;
+  size_t o_views = 0, o_lines = 0, o_off = 0, o_nnp = 0, o_lam = 0, o_ktab = 0, o_xy = 0, o_ctr = 0, o_s2 = 0;
+};
+
+struct Plan {
+  std::vector<PlanGroup> groups;
+  std::vector<int> view_of_req;
+  int nviews_total = 0;
+  size_t host_bytes = 0, dev_bytes = 0;
+  char* arena_base = nullptr;
+};
+
+struct ViewReadback {
+  ViewDesc* dev;
+  size_t base;
+  int count;
+};
+
+struct GraphRec {
+  cudaGraphExec_t exec = nullptr;
+};
+
+struct TuneChoice {
+  int tile_w = 8, tile_h = 4, blocks_per_sm = 0;
+};
+
+}  // namespace fomo
+
+struct fomo_ctx {
+  int device = 0;
+  int sm_count = 152;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  size_t used = 0;
+  std::map<void*, size_t> sizes;
+  int next_id = 1;
+  std::string err;
+  std::map<int, fomo::SnapRec> snaps;
+  std::map<int, fomo::TableRec> tables;
+  std::map<std::tuple<int, int, int, double>, float2*> payloads;
+  fomo::ScratchSet scratch;  // descriptors, per-view tables, Thomson sin^2 chi
+  fomo::Arena out_arena;     // device cubes of host-output renders
+  std::vector<fomo::ViewReadback> view_readback;
+  double cell_occupancy = 2.0;  // target points per grid cell
+  int tile_w = 0, tile_h = 0, blocks_per_sm = 0;
+  bool time_march = true;
+  float last_ms = 0.0f;
+  cudaEvent_t order_ev = nullptr;  // orders a caller stream after the context stream
+  std::map<std::string, fomo::GraphRec> graphs;
+  std::map<std::string, fomo::TuneChoice> tuned;
+};
+
+namespace fomo {
+
+int set_err(fomo_ctx* c, int code, const std::string& msg);
+int cuda_err(fomo_ctx* c, cudaError_t e, const char* what);
+int dev_alloc(fomo_ctx* ctx, void** p, size_t bytes);
+void dev_free(fomo_ctx* ctx, void* p);
+int validate(fomo_ctx* ctx, const fomo_request& q);
+size_t cube_elems(const fomo_request& q);
+int enqueue_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
+                  cudaStream_t s, std::vector<ViewDesc>* views_out, std::vector<int>* view_of_req);
+int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
+               ScratchSet* scr, Plan* plan);
+int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s);
+std::string workload_class(const PlanGroup& G, const SnapRec& snap);
+int order_streams(fomo_ctx* ctx, cudaStream_t s);
+int finish_views(fomo_ctx* ctx, std::vector<ViewDesc>* views);
+void view_info_from(const ViewDesc& V, const fomo_request& q, const TableHost* t, fomo_view_info* info);
+int parse_table_text(const std::string& text, TableHost* t, std::string* err);
+
+}  // namespace fomo

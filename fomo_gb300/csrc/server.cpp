@@ -1,0 +1,349 @@
+// Render server: continuous batching of render requests as they arrive.
+//
+// Requests are submitted from any thread into a FIFO.  A scheduler thread
+// owns the server's context and two launch slots, each with its own CUDA
+// stream and scratch set.  Whenever a slot is free it admits every queued
+// request that fits the HBM budget (output cube + descriptors) and the
+// in-flight cap, plans them as one batch (one persistent march per launch
+// group, shared neighbour lookups for requests with the same view) and
+// enqueues it on the slot's stream.  While one slot's batch runs, requests
+// that arrive meanwhile are admitted into the other slot, so their work
+// overlaps on the device.  Results go device -> pinned staging -> the
+// caller's buffer; each request records submit / admit / start / done times.
+//
+// A request is rendered by the same kernels, with the same per-ray work, as
+// when it is rendered alone: one warp owns one ray and nothing in a ray's
+// arithmetic depends on what else shares the launch.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/fomo_gpu.h"
+#include "runtime_internal.h"
+
+using namespace fomo;
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+enum class TState { kQueued, kRunning, kDone };
+
+struct Ticket {
+  fomo_request req{};
+  float* out_host = nullptr;
+  size_t out_bytes = 0;
+  size_t cost = 0;  // admission bytes
+  TState state = TState::kQueued;
+  bool cancelled = false;
+  int status = FOMO_OK;
+  double t_submit = 0, t_admit = 0, t_start = 0, t_done = 0;
+  size_t dev_off = 0, host_off = 0;
+};
+
+struct Slot {
+  ScratchSet scr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  Arena out;              // device cubes of the batch
+  char* pinned = nullptr; // host staging of the cubes
+  size_t pinned_cap = 0;
+  std::vector<uint64_t> ids;
+  bool busy = false;
+  double t_launch = 0;
+};
+
+}  // namespace
+
+struct fomo_server {
+  fomo_ctx* ctx = nullptr;
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv;       // wakes the scheduler
+  std::condition_variable done_cv;  // wakes waiters
+  std::deque<uint64_t> queue;
+  std::map<uint64_t, Ticket> tickets;
+  uint64_t next_ticket = 1;
+  size_t budget = 0;
+  size_t inflight_bytes = 0;
+  int max_inflight = 64;
+  int inflight = 0;
+  bool stop = false;
+  Slot slots[2];
+  std::string err;
+  double t0 = 0;
+};
+
+namespace {
+
+size_t request_cost(const fomo_request& q) {
+  // output cube + per-view descriptors and tables (generous)
+  return cube_elems(q) * sizeof(float) + (size_t)q.nz * 24 + (size_t)(q.nx + q.ny) * 8 + 64 * 1024;
+}
+
+void finish_slot(fomo_server* S, Slot& sl, int status) {
+  // called with S->mu held
+  const double t = now_s() - S->t0;
+  for (uint64_t id : sl.ids) {
+    auto it = S->tickets.find(id);
+    if (it == S->tickets.end()) continue;
+    Ticket& T = it->second;
+    if (status == FOMO_OK && !T.cancelled && T.out_host)
+      std::memcpy(T.out_host, sl.pinned + T.host_off, T.out_bytes);
+    T.status = T.cancelled ? FOMO_ECANCELLED : status;
+    T.state = TState::kDone;
+    T.t_done = t;
+    S->inflight_bytes -= T.cost;
+    S->inflight -= 1;
+  }
+  sl.ids.clear();
+  sl.busy = false;
+}
+
+// Launch the admitted requests `ids` on slot `sl`; called without S->mu held.
+int launch_slot(fomo_server* S, Slot& sl, std::vector<uint64_t>& ids, std::vector<fomo_request>& reqs,
+                std::vector<size_t>& out_bytes) {
+  fomo_ctx* ctx = S->ctx;
+  const int n = (int)reqs.size();
+  std::vector<size_t> doff(n), hoff(n);
+  size_t dtot = 0;
+  for (int i = 0; i < n; ++i) {
+    doff[i] = dtot;
+    dtot += (out_bytes[i] + 255) & ~size_t(255);
+  }
+  int rc = sl.out.reserve(ctx, dtot);
+  if (rc) return rc;
+  if (sl.pinned_cap < dtot) {
+    if (sl.pinned) cudaFreeHost(sl.pinned);
+    sl.pinned = nullptr;
+    sl.pinned_cap = 0;
+    if (cudaMallocHost(reinterpret_cast<void**>(&sl.pinned), dtot) != cudaSuccess)
+      return set_err(ctx, FOMO_ENOMEM, "pinned result staging");
+    sl.pinned_cap = dtot;
+  }
+  std::vector<float*> d(n);
+  for (int i = 0; i < n; ++i) d[i] = reinterpret_cast<float*>(sl.out.base + doff[i]);
+  Plan plan;
+  rc = plan_batch(ctx, reqs.data(), n, d.data(), nullptr, &sl.scr, &plan);
+  if (rc) return rc;
+  rc = order_streams(ctx, sl.stream);
+  if (rc) return rc;
+  rc = issue_plan(ctx, plan, &sl.scr, sl.stream);
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i) {
+    cudaError_t e = cudaMemcpyAsync(sl.pinned + doff[i], d[i], out_bytes[i], cudaMemcpyDeviceToHost, sl.stream);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "result download");
+  }
+  cudaError_t e = cudaEventRecord(sl.done, sl.stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "slot event");
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (int i = 0; i < n; ++i) {
+    auto it = S->tickets.find(ids[i]);
+    if (it != S->tickets.end()) it->second.host_off = doff[i];
+  }
+  return FOMO_OK;
+}
+
+void scheduler(fomo_server* S) {
+  cudaSetDevice(S->ctx->device);
+  for (;;) {
+    std::unique_lock<std::mutex> lk(S->mu);
+    // completions
+    for (Slot& sl : S->slots) {
+      if (!sl.busy) continue;
+      cudaError_t q = cudaEventQuery(sl.done);
+      if (q == cudaSuccess) {
+        finish_slot(S, sl, FOMO_OK);
+        S->done_cv.notify_all();
+      } else if (q != cudaErrorNotReady) {
+        S->err = std::string("device error: ") + cudaGetErrorString(q);
+        finish_slot(S, sl, FOMO_EDEVICE);
+        S->done_cv.notify_all();
+      }
+    }
+    const bool any_busy = S->slots[0].busy || S->slots[1].busy;
+    if (S->stop && S->queue.empty() && !any_busy) break;
+    // admission into a free slot
+    Slot* free_slot = !S->slots[0].busy ? &S->slots[0] : (!S->slots[1].busy ? &S->slots[1] : nullptr);
+    if (free_slot && !S->queue.empty()) {
+      std::vector<uint64_t> ids;
+      std::vector<fomo_request> reqs;
+      std::vector<size_t> out_bytes;
+      const double t = now_s() - S->t0;
+      while (!S->queue.empty()) {
+        uint64_t id = S->queue.front();
+        Ticket& T = S->tickets[id];
+        if (T.cancelled) {
+          S->queue.pop_front();
+          T.state = TState::kDone;
+          T.status = FOMO_ECANCELLED;
+          T.t_done = t;
+          S->done_cv.notify_all();
+          continue;
+        }
+        if (S->inflight > 0 && (S->inflight_bytes + T.cost > S->budget || S->inflight >= S->max_inflight)) break;
+        S->queue.pop_front();
+        T.state = TState::kRunning;
+        T.t_admit = t;
+        T.t_start = t;
+        S->inflight_bytes += T.cost;
+        S->inflight += 1;
+        ids.push_back(id);
+        reqs.push_back(T.req);
+        out_bytes.push_back(T.out_bytes);
+      }
+      if (!ids.empty()) {
+        free_slot->busy = true;
+        free_slot->ids = ids;
+        lk.unlock();
+        int rc = launch_slot(S, *free_slot, ids, reqs, out_bytes);
+        lk.lock();
+        if (rc != FOMO_OK) {
+          S->err = S->ctx->err;
+          finish_slot(S, *free_slot, rc);
+          S->done_cv.notify_all();
+        }
+        continue;
+      }
+    }
+    // nothing to launch: wait for a submission or poll the device
+    if (any_busy)
+      S->cv.wait_for(lk, std::chrono::microseconds(100));
+    else
+      S->cv.wait_for(lk, std::chrono::milliseconds(50));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fomo_server_create(const fomo_server_config* config, fomo_server** out) {
+  if (!config || !out) return FOMO_EINVAL;
+  *out = nullptr;
+  fomo_ctx* ctx = nullptr;
+  int rc = fomo_ctx_create(config->device, 0, &ctx);
+  if (rc) return rc;
+  fomo_server* S = new fomo_server();
+  S->ctx = ctx;
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  S->budget = config->hbm_budget_bytes ? config->hbm_budget_bytes : fr / 2;
+  S->max_inflight = config->max_inflight > 0 ? config->max_inflight : 64;
+  for (Slot& sl : S->slots) {
+    if (sl.scr.init() != cudaSuccess || cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) {
+      fomo_ctx_destroy(ctx);
+      delete S;
+      return FOMO_EDEVICE;
+    }
+  }
+  S->t0 = now_s();
+  S->worker = std::thread(scheduler, S);
+  *out = S;
+  return FOMO_OK;
+}
+
+fomo_ctx* fomo_server_context(fomo_server* srv) { return srv ? srv->ctx : nullptr; }
+
+int fomo_server_submit(fomo_server* S, const fomo_request* req, float* out_host, uint64_t* ticket) {
+  if (!S || !req || !ticket) return FOMO_EINVAL;
+  Ticket T;
+  T.req = *req;
+  T.out_host = out_host;
+  T.out_bytes = cube_elems(*req) * sizeof(float);
+  T.cost = request_cost(*req);
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (req->nx < 2 || req->ny < 2 || req->nz < 1 || req->nlambda < 1) {
+    S->err = "resolution must have nx >= 2, ny >= 2, nz >= 1, nlambda >= 1";
+    return FOMO_EINVAL;
+  }
+  if (T.cost > S->budget) {
+    S->err = "request needs " + std::to_string(T.cost) + " bytes, more than the server's HBM budget of " +
+             std::to_string(S->budget);
+    return FOMO_EADMISSION;
+  }
+  if (S->stop) {
+    S->err = "server is stopping";
+    return FOMO_ECANCELLED;
+  }
+  T.t_submit = now_s() - S->t0;
+  const uint64_t id = S->next_ticket++;
+  S->tickets[id] = T;
+  S->queue.push_back(id);
+  *ticket = id;
+  S->cv.notify_all();
+  return FOMO_OK;
+}
+
+int fomo_server_wait(fomo_server* S, uint64_t ticket, double timeout_s, fomo_request_stats* stats) {
+  if (!S) return FOMO_EINVAL;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->tickets.find(ticket);
+  if (it == S->tickets.end()) return FOMO_ENOTFOUND;
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+  while (S->tickets[ticket].state != TState::kDone) {
+    if (S->done_cv.wait_until(lk, deadline) == std::cv_status::timeout &&
+        S->tickets[ticket].state != TState::kDone)
+      return FOMO_ETIMEOUT;
+  }
+  Ticket& T = S->tickets[ticket];
+  if (stats) {
+    stats->t_submit = T.t_submit;
+    stats->t_admit = T.t_admit;
+    stats->t_start = T.t_start;
+    stats->t_done = T.t_done;
+    stats->status = T.status;
+  }
+  const int st = T.status;
+  S->tickets.erase(ticket);
+  return st;
+}
+
+int fomo_server_cancel(fomo_server* S, uint64_t ticket) {
+  if (!S) return FOMO_EINVAL;
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->tickets.find(ticket);
+  if (it == S->tickets.end()) return FOMO_ENOTFOUND;
+  it->second.cancelled = true;  // queued: dropped at admission; running: result discarded
+  S->cv.notify_all();
+  return FOMO_OK;
+}
+
+int fomo_server_destroy(fomo_server* S) {
+  if (!S) return FOMO_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+    S->cv.notify_all();
+  }
+  if (S->worker.joinable()) S->worker.join();
+  for (Slot& sl : S->slots) {
+    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    dev_free(S->ctx, sl.scr.arena.base);
+    dev_free(S->ctx, sl.out.base);
+    sl.scr.release();
+    if (sl.pinned) cudaFreeHost(sl.pinned);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
+  }
+  fomo_ctx_destroy(S->ctx);
+  delete S;
+  return FOMO_OK;
+}
+
+const char* fomo_server_last_error(fomo_server* S) { return S ? S->err.c_str() : "null server"; }
+
+}  // extern "C"

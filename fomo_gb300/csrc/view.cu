@@ -1,0 +1,202 @@
+// K3: per-view set-up, entirely on the device (no host round trip).
+//
+//  * view_extents_kernel: Stage A of the reference (fomo-c/src/fomo-nearest-
+//    neighbour.cpp:76-108): every point rotated in FP64 with the reference's
+//    operand order, min/max reduced through order-preserving 64-bit atomics
+//    (exact, order independent).  For Thomson the pole-blended rotation with
+//    clamped cos/sin and sin^2(chi) per point (fomo-thomson.cpp:139-199).
+//  * view_finalize_kernel: maxdistance (nn:138 / thomson:249-260), delta z,
+//    path length and DN pixel area (nn:235-267), and the per-LOS-sample FP64
+//    table z_k*sin(b)*cos(l), z_k*sin(b)*sin(l), z_k*cos(b) that the march
+//    adds to the per-ray terms -- the same roundings as the reference's
+//    derotation expression (nn:162-165).
+// Transcendentals (cos, sin, exp of the blends) are evaluated on the host with
+// the host libm and passed in; everything here is +, -, *, /, sqrt in IEEE
+// FP64 with explicit round-to-nearest intrinsics (no FMA contraction).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fomo_internal.h"
+
+namespace fomo {
+
+namespace {
+
+__device__ __forceinline__ unsigned long long d2ord(double d) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord2d(unsigned long long u) {
+  u = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+  return __longlong_as_double((long long)u);
+}
+
+__global__ void view_init_kernel(ViewDesc* views, int nviews) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nviews) return;
+  for (int d = 0; d < 3; ++d) {
+    views[v].ext_bits[2 * d] = 0xffffffffffffffffull;  // min
+    views[v].ext_bits[2 * d + 1] = 0ull;                // max
+  }
+}
+
+__device__ __forceinline__ void warp_minmax(unsigned long long& mn, unsigned long long& mx) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long a = __shfl_xor_sync(0xffffffffu, mn, o);
+    unsigned long long b = __shfl_xor_sync(0xffffffffu, mx, o);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+}
+
+// grid: (blocks over points, views)
+__global__ void view_extents_kernel(SnapDev snap, ViewDesc* views, float* s2) {
+  ViewDesc* V = views + blockIdx.y;
+  const double cb = V->rcb, sb = V->rsb, cl = V->cl, sl = V->sl;
+  const bool thomson = V->method == kMethodThomson;
+  const double blend = V->blend;
+  const double omb = __dsub_rn(1.0, blend);
+  unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
+  float* s2v = s2 ? s2 + (int64_t)blockIdx.y * snap.n : nullptr;
+  // LOS unit for sin^2 chi (thomson:194): clamped sin_b/cos_b with cos(l), sin(l)
+  const double u0 = __dmul_rn(sb, cl), u1 = __dmul_rn(-sb, sl), u2 = cb;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < snap.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 p = snap.pts[i];
+    const double gx = p.x, gy = p.y, gz = p.z;
+    // full rotation (nn:83-85, thomson:179-181)
+    double xa = __dsub_rn(__dsub_rn(__dmul_rn(__dmul_rn(gx, cb), cl), __dmul_rn(__dmul_rn(gy, cb), sl)),
+                          __dmul_rn(gz, sb));
+    double ya = __dadd_rn(__dmul_rn(gx, sl), __dmul_rn(gy, cl));
+    double za = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(gx, sb), cl), __dmul_rn(__dmul_rn(gy, sb), sl)),
+                          __dmul_rn(gz, cb));
+    if (thomson) {
+      // pole rotation and blend (thomson:184-191)
+      const double pxr = __dsub_rn(__dmul_rn(gx, cl), __dmul_rn(gy, sl));
+      const double pyr = __dadd_rn(__dmul_rn(gx, sl), __dmul_rn(gy, cl));
+      const double pzr = gz;
+      xa = __dadd_rn(__dmul_rn(xa, omb), __dmul_rn(pxr, blend));
+      ya = __dadd_rn(__dmul_rn(ya, omb), __dmul_rn(pyr, blend));
+      za = __dadd_rn(__dmul_rn(za, omb), __dmul_rn(pzr, blend));
+      // sin^2 chi = 1 - (u.r)^2 / (r.r)  (thomson:194-199)
+      double ip = __dmul_rn(u0, xa);
+      ip = __dadd_rn(ip, __dmul_rn(u1, ya));
+      ip = __dadd_rn(ip, __dmul_rn(u2, za));
+      double pp = __dmul_rn(xa, xa);
+      pp = __dadd_rn(pp, __dmul_rn(ya, ya));
+      pp = __dadd_rn(pp, __dmul_rn(za, za));
+      s2v[i] = __double2float_rn(__dsub_rn(1.0, __ddiv_rn(__dmul_rn(ip, ip), pp)));
+    }
+    const unsigned long long ex = d2ord(xa), ey = d2ord(ya), ez = d2ord(za);
+    mn[0] = ex < mn[0] ? ex : mn[0];
+    mx[0] = ex > mx[0] ? ex : mx[0];
+    mn[1] = ey < mn[1] ? ey : mn[1];
+    mx[1] = ey > mx[1] ? ey : mx[1];
+    mn[2] = ez < mn[2] ? ez : mn[2];
+    mx[2] = ez > mx[2] ? ez : mx[2];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) warp_minmax(mn[d], mx[d]);
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      atomicMin(&V->ext_bits[2 * d], mn[d]);
+      atomicMax(&V->ext_bits[2 * d + 1], mx[d]);
+    }
+  }
+}
+
+__device__ __forceinline__ double dmax_ref(double a, double b) { return (a < b) ? b : a; }  // std::max
+
+// One block per view.
+__global__ void view_finalize_kernel(ViewDesc* views, double3* ktab, int ktab_stride) {
+  ViewDesc* V = views + blockIdx.x;
+  __shared__ double s_dz, s_minz;
+  if (threadIdx.x == 0) {
+    const double minx = ord2d(V->ext_bits[0]), maxx = ord2d(V->ext_bits[1]);
+    const double miny = ord2d(V->ext_bits[2]), maxy = ord2d(V->ext_bits[3]);
+    const double minz = ord2d(V->ext_bits[4]), maxz = ord2d(V->ext_bits[5]);
+    V->minx = minx;
+    V->maxx = maxx;
+    V->miny = miny;
+    V->maxy = maxy;
+    V->minz = minz;
+    V->maxz = maxz;
+    const double dxr = __dsub_rn(maxx, minx), dyr = __dsub_rn(maxy, miny);
+    V->dxr = dxr;
+    V->dyr = dyr;
+    const double px = __ddiv_rn(dxr, (double)(V->nx - 1)), py = __ddiv_rn(dyr, (double)(V->ny - 1));
+    double md;
+    if (V->method == kMethodThomson) {
+      const double eq = dmax_ref(__dmul_rn(0.5, __dsqrt_rn(__dadd_rn(__dmul_rn(px, px), __dmul_rn(py, py)))),
+                                 __ddiv_rn(__dmul_rn(0.1, dxr), (double)(V->nx - 1)));
+      const double away = __ddiv_rn(dmax_ref(px, py), 0.005);
+      md = __dadd_rn(__dmul_rn(eq, __dsub_rn(1.0, V->mdblend)), __dmul_rn(away, V->mdblend));
+    } else {
+      md = __ddiv_rn(dmax_ref(px, py), .3);
+    }
+    V->md = md;
+    double deltaz = __dsub_rn(maxz, minz);
+    if (V->nz != 1) deltaz = __ddiv_rn(deltaz, (double)(V->nz - 1));
+    V->deltaz = deltaz;
+    double pathlength = __ddiv_rn(__dsub_rn(maxz, minz), (double)(V->nz - 1));
+    if (maxz == minz || V->nz == 1) pathlength = 1.0;
+    V->pathlength = pathlength;
+    double apix = 1.0;
+    {
+      const float dxf = __double2float_rn(px), dyf = __double2float_rn(py);
+      const double as = FOMO_PI / 180. / 3600.;
+      apix = __dmul_rn(__dmul_rn(__ddiv_rn((double)dxf, FOMO_MM_PER_ARCSEC), __ddiv_rn((double)dyf, FOMO_MM_PER_ARCSEC)),
+                       __dmul_rn(as, as));
+    }
+    V->apix = apix;
+    V->scale = __dmul_rn(__dmul_rn(pathlength, 1e8), 1.0);
+    V->scale_dn = __dmul_rn(__dmul_rn(pathlength, 1e8), apix);
+    V->lwa = __ddiv_rn(__dmul_rn(V->lambda_width, V->lambda0), FOMO_SPEED_OF_LIGHT);
+    V->ux = __double2float_rn(__dmul_rn(V->sb, V->cl));
+    V->uy = __double2float_rn(__dmul_rn(-V->sb, V->sl));
+    V->uz = __double2float_rn(V->cb);
+    s_dz = deltaz;
+    s_minz = minz;
+  }
+  __syncthreads();
+  const double cb = V->cb, sb = V->sb, cl = V->cl, sl = V->sl;
+  const double dz = s_dz, minz = s_minz;
+  // ray positions in the image plane (nn:152-153)
+  for (int j = threadIdx.x; j < V->nx; j += blockDim.x)
+    V->xt[j] = __dadd_rn(__dmul_rn(__ddiv_rn((double)j, (double)(V->nx - 1)), V->dxr), V->minx);
+  for (int i = threadIdx.x; i < V->ny; i += blockDim.x)
+    V->yt[i] = __dadd_rn(__dmul_rn(__ddiv_rn((double)i, (double)(V->ny - 1)), V->dyr), V->miny);
+  double3* kt = ktab + (int64_t)blockIdx.x * ktab_stride;
+  for (int k = threadIdx.x; k < V->nz; k += blockDim.x) {
+    const double z = __dadd_rn(__dmul_rn((double)k, dz), minz);  // nn:162
+    const double zsb = __dmul_rn(z, sb);
+    kt[k] = make_double3(__dmul_rn(zsb, cl), __dmul_rn(zsb, sl), __dmul_rn(z, cb));
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_view_init(ViewDesc* views, int nviews, cudaStream_t s) {
+  view_init_kernel<<<(nviews + 127) / 128, 128, 0, s>>>(views, nviews);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_view_extents(SnapDev snap, ViewDesc* views, int nviews, float* s2, cudaStream_t s) {
+  int64_t blocks = (snap.n + 255) / 256;
+  int64_t cap = (152 * 8 + nviews - 1) / nviews;
+  if (cap < 8) cap = 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  dim3 grid((unsigned)blocks, (unsigned)nviews);
+  view_extents_kernel<<<grid, 256, 0, s>>>(snap, views, s2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_view_finalize(ViewDesc* views, int nviews, double3* ktab, int ktab_stride, cudaStream_t s) {
+  view_finalize_kernel<<<nviews, 256, 0, s>>>(views, ktab, ktab_stride);
+  return cudaGetLastError();
+}
+
+}  // namespace fomo

@@ -1,0 +1,145 @@
+"""GPU: batched launches, CUDA-graph replay, the render server, and a
+full-size parity sample.  Every result must equal the same request rendered
+alone (one warp owns one ray, so mixing cannot change a ray's arithmetic)."""
+
+import math
+import threading
+
+import numpy as np
+import pytest
+
+import fomo_gb300 as fg
+import oracle
+from fomo_gb300 import synth
+from tests import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = fg.Context(0)
+    yield c
+    c.close()
+
+
+def _mixed_requests(sid, tids, bb, rng, n):
+    reqs = []
+    for _ in range(n):
+        kind = rng.integers(0, 3)
+        nx = int(rng.choice([8, 16, 32, 48]))
+        ny = int(rng.choice([8, 16, 24]))
+        nz = int(rng.choice([7, 32, 64]))
+        l, b = float(rng.uniform(0, math.pi)), float(rng.uniform(-0.6, 0.6))
+        if kind == 0:
+            reqs.append(fg.Context.request(sid, int(rng.choice(tids)), fg.METHOD_NN, nx, ny, nz,
+                                           int(rng.choice([16, 64, 128])), l, b, 1.5e5))
+        elif kind == 1:
+            reqs.append(fg.Context.request(sid, bb, fg.METHOD_NN, nx, ny, nz, 1, l, b, 1e5))
+        else:
+            reqs.append(fg.Context.request(sid, int(rng.choice(tids)), fg.METHOD_NN, nx, ny, nz, 40, l, b, 9e4))
+    return reqs
+
+
+def test_graph_replay_equals_direct(ctx):
+    import torch
+    s = synth.loop_snapshot(20, seed=9)
+    sid = ctx.snapshot(s)
+    tids = [ctx.table(synth.line_table(peak_logT=p, lambda0=lam)) for p, lam in ((5.9, 171.0), (6.1, 195.0))]
+    dev = torch.device("cuda", 0)
+    for (l, b) in [(0.2, 0.1), (1.1, -0.4), (2.0, 0.3)]:  # same shape: captured once, replayed
+        reqs = [ctx.request(sid, t, fg.METHOD_NN, 24, 20, 48, 32, l, b, 1.4e5) for t in tids]
+        outs = [torch.empty((20, 24, 32), dtype=torch.float32, device=dev) for _ in reqs]
+        ctx.render_batch_device(reqs, [o.data_ptr() for o in outs], graph=True)
+        ctx.synchronize()
+        for q, o in zip(reqs, outs):
+            single, _, _ = ctx.render(q)
+            np.testing.assert_array_equal(o.cpu().numpy(), single)
+    ctx.drop_snapshot(sid)
+
+
+def test_server_same_alone_and_in_mix():
+    rng = np.random.default_rng(17)
+    with fg.Server(0) as srv:
+        c = srv.ctx
+        s = synth.loop_snapshot(24, seed=3)
+        sid = c.snapshot(s)
+        tids = [c.table(synth.line_table(peak_logT=p, lambda0=lam)) for p, lam in ((5.8, 171.0), (6.2, 211.0))]
+        bb = c.table(synth.broadband_table(171))
+        reqs = _mixed_requests(sid, tids, bb, rng, 24)
+        alone = []
+        for q in reqs:
+            out = np.empty(fg.Context.cube_shape(q), np.float32)
+            st = srv.wait(srv.submit(q, out))
+            assert st.status == fg.OK
+            alone.append(out)
+        # all at once, from several threads
+        mixed = [np.empty(fg.Context.cube_shape(q), np.float32) for q in reqs]
+        tickets = [None] * len(reqs)
+
+        def sub(idx):
+            for i in idx:
+                tickets[i] = srv.submit(reqs[i], mixed[i])
+
+        th = [threading.Thread(target=sub, args=(list(range(k, len(reqs), 4)),)) for k in range(4)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        stats = [srv.wait(t) for t in tickets]
+        for a, m, st in zip(alone, mixed, stats):
+            assert st.status == fg.OK and st.t_done >= st.t_submit
+            np.testing.assert_array_equal(a, m)
+
+
+def test_server_admission_rejects_oversized_request():
+    with fg.Server(0, hbm_budget=64 << 20) as srv:
+        sid = srv.ctx.snapshot(synth.loop_snapshot(8, seed=1))
+        tid = srv.ctx.table(synth.line_table())
+        big = fg.Context.request(sid, tid, fg.METHOD_NN, 1024, 1024, 64, 128, 0.0, 0.0, 1e5)  # 512 MB cube
+        with pytest.raises(fg.FomoError) as ei:
+            srv.submit(big, np.empty(1, np.float32))
+        assert ei.value.code == fg.EADMISSION
+        ok = fg.Context.request(sid, tid, fg.METHOD_NN, 16, 16, 16, 16, 0.0, 0.0, 1e5)
+        out = np.empty((16, 16, 16), np.float32)
+        assert srv.wait(srv.submit(ok, out)).status == fg.OK
+
+
+def test_unknown_ids_and_bad_arguments(ctx):
+    with pytest.raises(fg.FomoError) as ei:
+        ctx.render(ctx.request(12345, 0, fg.METHOD_NN, 8, 8, 8, 8))
+    assert ei.value.code == fg.ENOTFOUND
+    sid = ctx.snapshot(synth.loop_snapshot(6, seed=1))
+    with pytest.raises(fg.FomoError) as ei:
+        ctx.render(ctx.request(sid, 0, 7, 8, 8, 8, 8))
+    assert ei.value.code == fg.EMETHOD
+    with pytest.raises(fg.FomoError) as ei:
+        ctx.render(ctx.request(sid, 0, fg.METHOD_THOMSON, 1, 8, 8, 1))
+    assert ei.value.code == fg.EINVAL
+    with pytest.raises(fg.FomoError) as ei:
+        ctx.load_table("/nonexistent/table.dat")
+    assert ei.value.code == fg.EIO
+    ctx.drop_snapshot(sid)
+
+
+def test_full_size_plain_config_sampled_rows(ctx):
+    """128^3 = 2,097,152 points, 512x512 pixels, 128 bins, 512 samples, l = 30 deg:
+    neighbour indices of sampled image rows bit-exact, their spectra within 1e-4."""
+    s = synth.loop_snapshot(128, seed=1)
+    t = synth.line_table()
+    sid = ctx.snapshot(s)
+    tid = ctx.table(t)
+    width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+    l = math.radians(30.0)
+    req = ctx.request(sid, tid, fg.METHOD_NN, 512, 512, 512, 128, l, 0.0, width)
+    cube, idx, info = ctx.render(req, want_idx=True)
+    eps, w = oracle.emission(s, t)
+    for r0 in (3, 255, 509):
+        oc, oi, ov = oracle.nn_render(s, eps, w, t.lambda0, l, 0.0, 512, 512, 512, 128, width, rows=(r0, r0 + 2),
+                                      want_idx=True)
+        np.testing.assert_array_equal(idx[r0:r0 + 2], oi)
+        assert info.maxdistance == ov[oracle.V_MAXDIST]
+        if np.abs(oc).max() > 0:
+            assert G.norm_max_err(cube[r0:r0 + 2].ravel(), oc.ravel()) <= 1e-4
+    assert (idx >= 0).mean() > 0.5
+    ctx.drop_snapshot(sid)
