@@ -83,6 +83,9 @@ int fomo_render_batch_graph(fomo_ctx* ctx, const fomo_request* reqs, int nreq, f
   }
   cudaError_t e = cudaGraphLaunch(it->second.exec, s);
   if (e != cudaSuccess) return cuda_err(ctx, e, "graph launch");
+  // the staging blob may be rewritten once this launch (and its upload) has run
+  e = cudaEventRecord(ctx->scratch.staging.copy_done, s);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "graph launch");
   return FOMO_OK;
 }
 

@@ -108,6 +108,38 @@ __global__ void thomson_emission_kernel(const float4* __restrict__ pts, const fl
   }
 }
 
+// Largest line width among points that emit (eps != 0): bounds the lambda
+// window the march evaluates.  Non-negative floats order like their bits; NaN
+// and inf map to +inf (the host then evaluates every bin).
+__global__ void payload_stats_kernel(const float2* __restrict__ ew, int64_t n, unsigned int* wmax_bits) {
+  unsigned int m = 0u;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = ew[i];
+    if (v.x != 0.0f) {
+      float w = fabsf(v.y);
+      if (!(w <= 3.0e38f)) w = __int_as_float(0x7f800000);
+      m = max(m, __float_as_uint(w));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(wmax_bits, m);
+}
+
+// Largest speed |v| of a snapshot: bounds the Doppler shift of every LOS.
+__global__ void speed_max_kernel(const float4* __restrict__ vel, int64_t n, unsigned int* vmax_bits) {
+  unsigned int m = 0u;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 v = vel[i];
+    float s = sqrtf(fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x))) * 1.0001f;
+    if (!(s <= 3.0e38f)) s = __int_as_float(0x7f800000);
+    m = max(m, __float_as_uint(s));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(vmax_bits, m);
+}
+
 // Sorted payload back to the caller's point order: out[orig(i)] = ew[i].
 __global__ void unsort_kernel(const float4* __restrict__ pts, const float2* __restrict__ ew, int64_t n,
                               float* __restrict__ a, float* __restrict__ b) {
@@ -141,6 +173,20 @@ cudaError_t launch_emission(const float* ne_s, const float* T_s, int64_t n, Tabl
   } else {
     emission_kernel<false><<<blocks_for(n, 256), 256, 0, s>>>(ne_s, T_s, n, t, ew);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_payload_stats(const float2* ew, int64_t n, unsigned int* wmax_bits, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(wmax_bits, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  payload_stats_kernel<<<blocks_for(n, 256), 256, 0, s>>>(ew, n, wmax_bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_speed_max(const float4* vel, int64_t n, unsigned int* vmax_bits, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(vmax_bits, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  speed_max_kernel<<<blocks_for(n, 256), 256, 0, s>>>(vel, n, vmax_bits);
   return cudaGetLastError();
 }
 

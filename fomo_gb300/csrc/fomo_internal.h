@@ -71,6 +71,8 @@ struct LineDesc {
   double lwa;                // lambda_width * lambda0 / c (Angstrom)
   float shift_k;             // lambda0 / c in FP32 (Doppler shift per m/s)
   int is_dn;                 // unit contains "DN": per-pixel scaling
+  int wstart;                // first lambda bin of the evaluated window
+  int nw;                    // 32-bin windows evaluated; other bins are below 2^-64 of every peak
 };
 
 struct MarchArgs {
@@ -86,6 +88,21 @@ struct MarchArgs {
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
   unsigned int* err;             // device error word (bounds-check builds)
+  unsigned long long* stats;     // optional search counters (FOMO_MARCH_STATS=1), else null
+};
+
+// Search counters accumulated when MarchArgs::stats is set.
+enum MarchStat {
+  kStatSegments = 0,   // 64-sample segments searched
+  kStatCandidates,     // candidates gathered
+  kStatRows,           // cell rows visited by the gather
+  kStatPointsLoaded,   // points loaded by the gather
+  kStatNotGathered,    // segments that fell back entirely (too many rows / candidates)
+  kStatFallbacks,      // samples resolved by the per-lane ring search
+  kStatSamples,        // LOS samples searched
+  kStatScanned,        // candidates scanned by samples
+  kStatTies,           // samples re-ranked in FP64
+  kStatCount
 };
 
 // ---------------------------------------------------------------------------
@@ -121,6 +138,8 @@ cudaError_t launch_thomson_emission(const float4* pts, const float* ne_s, int64_
                                     cudaStream_t s);
 cudaError_t launch_unsort_payload(const float4* pts, const float2* ew, int64_t n, float* a, float* b,
                                   cudaStream_t s);
+cudaError_t launch_payload_stats(const float2* ew, int64_t n, unsigned int* wmax_bits, cudaStream_t s);
+cudaError_t launch_speed_max(const float4* vel, int64_t n, unsigned int* vmax_bits, cudaStream_t s);
 
 // view.cu
 cudaError_t launch_view_init(ViewDesc* views, int nviews, cudaStream_t s);
@@ -128,8 +147,8 @@ cudaError_t launch_view_extents(SnapDev snap, ViewDesc* views, int nviews, float
 cudaError_t launch_view_finalize(ViewDesc* views, int nviews, double3* ktab, int ktab_stride, cudaStream_t s);
 
 // march.cu
-cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_L, int sm_count,
-                         cudaStream_t s, int blocks_per_sm_hint);
+cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
+                         cudaStream_t s, int blocks_per_sm_hint, bool imaging);
 int march_bins_per_lane(int nlines, int L);
 
 }  // namespace fomo

@@ -3,26 +3,47 @@
 // (view, ray) work items so that many views and requests share one launch.
 //
 // Per ray: the FP64 per-ray terms of the derotation (x cos b cos l + y sin l,
-// -x cos b sin l + y cos l, -x sin b) are formed once; lane k of each 32-sample
-// chunk adds the per-sample FP64 table entry of its LOS sample, rounds the
-// target and the box corners p -+ maxdistance to FP32 exactly as the reference
-// does (nn:171,179), and finds the nearest point strictly inside the box.
+// -x cos b sin l + y cos l, -x sin b) are formed once; each LOS sample adds the
+// FP64 table entry of its index (z_k sin b cos l, ...) and rounds the target to
+// FP32 exactly as the reference does (nn:162-171).
 //
-// Neighbour search: rings of grid cells around the target's cell, clipped to
-// the box's cell range, x-rows scanned as contiguous point ranges, stopped by
-// a conservative ring / row / cell distance bound.  Distances are compared in
-// FP32 with the two best kept; when they are within 4e-6 relative (a possible
-// tie under the reference's FP64 distance), the candidates are re-ranked with
-// the exact FP64 distance in Boost's order (dz^2 + (dy^2 + dx^2)) and the
-// lowest original index -- so the chosen neighbour equals the FP64 argmin.
+// Neighbour search, per 64-sample segment of a ray (warp-cooperative; lane i
+// owns samples i and i+32 of the segment):
+//  1. gather: the segment's targets lie on one line.  Every x-row of grid
+//     cells that can hold a point within R of the segment gets the x-range of
+//     cells the segment passes near; the rows' point ranges are prefix-summed
+//     across the warp and loaded 32 points per round (balanced), and points
+//     within R are compacted into a per-warp shared-memory list with the index
+//     of the sample they project onto.  R = min(sqrt(3) * maxdistance,
+//     1.15 local point spacings), the local spacing estimated from the cells the
+//     segment crosses;
+//  2. bucket sort: the list is counting-sorted by that sample index;
+//  3. scan: each sample tests the candidates of the buckets within R of it:
+//     FP32 squared distance, and the Chebyshev distance against maxdistance
+//     for the strict box of nn:179 (a candidate within a few ulp of a box face
+//     makes the sample "ambiguous");
+//  4. accept: a winner is final when it lies within the sample's coverage
+//     radius (points farther than R from the segment cannot be nearer) and no
+//     candidate was ambiguous; "no neighbour" is final when the box lies outside
+//     the points' bounding box or inside the covered ball.  Near-ties (two best
+//     FP32 distances within 4e-6) are re-ranked with the exact FP64 distance in
+//     Boost's order (dz^2 + (dy^2 + dx^2)) and the lowest original index;
+//  5. fallback: every other sample (about 1 %) is resolved by the whole warp
+//     together: rings of grid cells around the sample's cell, clipped to its
+//     box (corners rounded from FP64 as the reference does), rows flattened
+//     across the lanes, stopped by a conservative distance bound, warp argmin.
+// Either way the chosen neighbour is the FP64 argmin strictly inside the box.
 //
 // Spectroscopic mode: equal neighbours of consecutive samples are merged into
-// runs (warp ballot), and each run adds count * eps * 2^(-(2 (lambda - shift)/w)^2)
-// (= eps exp(-4 ln2 (dlambda/w)^2), nn:204) to the lane-owned lambda bins of
-// every line with FP32 Kahan sums.  Imaging (L = 1) and Thomson (pB) modes add
-// the per-sample value through a warp reduction.  One warp owns one ray: no
-// atomics on the output, results are deterministic and independent of what
-// else shares the launch.
+// runs (warp ballot); the lane starting a run loads its payload and forms, per
+// line, count * eps, 2 / w and the Doppler term; every lane then adds
+// count * eps * 2^(-(2 (lambda - shift) / w)^2)  (= eps exp(-4 ln2 (dl/w)^2),
+// nn:204) to its lambda bins of the line's window (the bins where any point's
+// Gaussian can exceed 2^-64 of its peak; the others are written as 0) in a
+// per-chunk FP32 partial, folded into the per-ray sum with Kahan compensation.
+// Imaging (L = 1) and Thomson (pB) add per-sample values through a warp
+// reduction.  One warp owns one ray: no atomics on the output; results are
+// deterministic and independent of what else shares the launch.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
@@ -35,19 +56,32 @@ namespace fomo {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kThreads = 256;
-constexpr float kRelTie = 4e-6f;    // FP32 distance ambiguity band (>> FP32 + FP64 error)
-constexpr float kRelPrune = 1e-5f;  // pruning slack on the squared distance
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr float kRelTie = 4e-6f;      // FP32 distance ambiguity band (>> FP32 + FP64 error)
+constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
+constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
+constexpr int kSegCap = 256;          // candidates per segment
+constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule before the cooperative fallback
+constexpr float kRScale = 1.15f;      // gather radius in local point spacings
 
-struct Best {
-  float d1, d2;  // two smallest FP32 squared distances
-  int pos;       // sorted position of d1
-  int orig;      // original index of d1
+struct __align__(16) SegSmem {
+  float4 cq[kSegCap];  // gathered candidates
+  float4 sq[kSegCap];  // candidates sorted by the sample they project onto
+  int cpos[kSegCap];
+  int spos[kSegCap];
+  int bstart[kSeg + 1];
+  int cursor[kSeg];
+  unsigned char cb[kSegCap];
 };
 
 struct BoxQ {
   float tx, ty, tz, lox, loy, loz, hix, hiy, hiz;
+};
+
+struct CellRange {
+  int b0[3], b1[3], c[3];
 };
 
 __device__ __forceinline__ float axis_gap(int c, float t, float o, float h) {
@@ -56,61 +90,57 @@ __device__ __forceinline__ float axis_gap(int c, float t, float o, float h) {
   return fmaxf(fmaxf(lo - t, t - hi), 0.0f);
 }
 
-__device__ __forceinline__ double exact_dist2(float px, float py, float pz, const BoxQ& q) {
-  const double dx = __dsub_rn((double)px, (double)q.tx);
-  const double dy = __dsub_rn((double)py, (double)q.ty);
-  const double dz = __dsub_rn((double)pz, (double)q.tz);
+__device__ __forceinline__ double exact_dist2(float px, float py, float pz, float tx, float ty, float tz) {
+  const double dx = __dsub_rn((double)px, (double)tx);
+  const double dy = __dsub_rn((double)py, (double)ty);
+  const double dz = __dsub_rn((double)pz, (double)tz);
   return __dadd_rn(__dmul_rn(dz, dz), __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dx, dx)));
 }
 
-// Scan points [b, e).  EXACT = false: FP32 two-best.  EXACT = true: FP64
-// re-rank of the candidates whose FP32 distance is within the tie band.
-template <bool EXACT>
-__device__ __forceinline__ void scan_range(const float4* __restrict__ pts, int b, int e, const BoxQ& q, Best& B,
-                                           float band, double& bestD, int& bestOrig, int& bestPos) {
-  for (int p = b; p < e; ++p) {
-    const float4 v = __ldg(pts + p);
-    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-      const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      if (!EXACT) {
-        if (d < B.d1) {
-          B.d2 = B.d1;
-          B.d1 = d;
-          B.pos = p;
-          B.orig = __float_as_int(v.w);
-        } else if (d < B.d2) {
-          B.d2 = d;
-        }
-      } else if (d <= band) {
-        const double D = exact_dist2(v.x, v.y, v.z, q);
-        const int o = __float_as_int(v.w);
-        if (D < bestD || (D == bestD && o < bestOrig)) {
-          bestD = D;
-          bestOrig = o;
-          bestPos = p;
-        }
-      }
-    }
-  }
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
 }
 
-// One pass of the ring search.  In the exact pass `bound` is fixed (the first
-// pass's best), in the first pass it shrinks as B.d1 improves.
-struct CellRange {
-  int b0[3], b1[3], c[3];
-};
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
 
+// Lane owning flattened item i: the number of lanes whose inclusive prefix is <= i.
+__device__ __forceinline__ int warp_owner(int incl, int i) {
+  int own = 0;
+#pragma unroll
+  for (int step = 16; step >= 1; step >>= 1) {
+    const int v = __shfl_sync(kFull, incl, own + step - 1);
+    if (v <= i) own += step;
+  }
+  return own;
+}
+
+// ---------------------------------------------------------------------------
+// Cooperative exact search for one sample (the fallback path).  All lanes
+// hold the same box; the rings of cells around the target's cell are walked
+// together, each ring's rows flattened across the lanes.
+// ---------------------------------------------------------------------------
 template <bool EXACT>
-__device__ __forceinline__ void ring_pass(const SnapDev& S, const BoxQ& q, const CellRange& R, Best& B, float band,
-                                          double& bestD, int& bestOrig, int& bestPos) {
+__device__ __forceinline__ void coop_ring_pass(const SnapDev& S, const BoxQ& q, const CellRange& R, float& gbest,
+                                               float band, float& lb1, float& lb2, int& lpos, int& lorig,
+                                               double& lD, int& lDorig, int& lDpos) {
+  const int lane = threadIdx.x & 31;
   const int* b0 = R.b0;
   const int* b1 = R.b1;
   const int* c = R.c;
   const GridParams& g = S.g;
   const float h = g.h;
   for (int s = 0;; ++s) {
-    const float bound = EXACT ? band * (1.0f + kRelPrune) : B.d1 * (1.0f + kRelPrune);
+    const float bound = EXACT ? band * (1.0f + kRelPrune) : gbest * (1.0f + kRelPrune);
     if (s >= 2) {
       const float lb = ((float)s - 1.0f - 2.0f * kCellMargin) * h;
       if (lb * lb > bound) break;
@@ -120,74 +150,101 @@ __device__ __forceinline__ void ring_pass(const SnapDev& S, const BoxQ& q, const
       break;
     const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
     const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
-    for (int kz = z0; kz <= z1; ++kz) {
-      const bool onz = (kz == c[2] - s) || (kz == c[2] + s);
-      const float gz = axis_gap(kz, q.tz, g.oz, h);
-      const float gz2 = gz * gz;
-      if (gz2 > (EXACT ? band * (1.0f + kRelPrune) : B.d1 * (1.0f + kRelPrune))) continue;
-      for (int jy = y0; jy <= y1; ++jy) {
+    const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
+    for (int rb = 0; rb < nrows; rb += 32) {
+      const int rr = rb + lane;
+      int baseA = 0, nA = 0, baseB = 0, nB = 0;
+      if (rr < nrows) {
+        const int kz = z0 + rr / nyr, jy = y0 + rr % nyr;
+        const bool onz = (kz == c[2] - s) || (kz == c[2] + s);
         const bool ony = (jy == c[1] - s) || (jy == c[1] + s);
-        const float gy = axis_gap(jy, q.ty, g.oy, h);
-        const float gyz = fmaf(gy, gy, gz2);
-        const float bnd = EXACT ? band * (1.0f + kRelPrune) : B.d1 * (1.0f + kRelPrune);
-        if (gyz > bnd) continue;
-        const int rowbase = (kz * g.dy + jy) * g.dx;
-        if (onz || ony) {
-          int x0 = max(c[0] - s, b0[0]), x1 = min(c[0] + s, b1[0]);
-          if (bnd < FLT_MAX) {
-            // clip the row to cells within sqrt(bnd - gyz) of the target in x
-            const float rem = fmaxf(bnd - gyz, 0.0f);
-            const float r = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
-            x0 = max(x0, cell_coord(q.tx - r, g.ox, g.inv_h, g.dx));
-            x1 = min(x1, cell_coord(q.tx + r, g.ox, g.inv_h, g.dx));
-          }
-          if (x0 <= x1) {
-            const int pb = __ldg(S.cell_start + rowbase + x0), pe = __ldg(S.cell_start + rowbase + x1 + 1);
-            scan_range<EXACT>(S.pts, pb, pe, q, B, band, bestD, bestOrig, bestPos);
-          }
-        } else {
-          const int xl = c[0] - s, xr = c[0] + s;
-          if (xl >= b0[0]) {
-            const float gx = axis_gap(xl, q.tx, g.ox, h);
-            if (fmaf(gx, gx, gyz) <= bnd) {
-              const int pb = __ldg(S.cell_start + rowbase + xl), pe = __ldg(S.cell_start + rowbase + xl + 1);
-              scan_range<EXACT>(S.pts, pb, pe, q, B, band, bestD, bestOrig, bestPos);
+        const float gz = axis_gap(kz, q.tz, g.oz, h), gy = axis_gap(jy, q.ty, g.oy, h);
+        const float gyz = fmaf(gy, gy, gz * gz);
+        if (gyz <= bound) {
+          const int rowbase = (kz * g.dy + jy) * g.dx;
+          if (onz || ony) {
+            int x0 = max(c[0] - s, b0[0]), x1 = min(c[0] + s, b1[0]);
+            if (bound < FLT_MAX) {
+              // clip the row to cells within sqrt(bound - gyz) of the target in x
+              const float rem = fmaxf(bound - gyz, 0.0f);
+              const float rx = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
+              x0 = max(x0, cell_coord(q.tx - rx, g.ox, g.inv_h, g.dx));
+              x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
+            }
+            if (x0 <= x1) {
+              baseA = __ldg(S.cell_start + rowbase + x0);
+              nA = __ldg(S.cell_start + rowbase + x1 + 1) - baseA;
+            }
+          } else {
+            const int xl = c[0] - s, xr = c[0] + s;
+            if (xl >= b0[0]) {
+              const float gx = axis_gap(xl, q.tx, g.ox, h);
+              if (fmaf(gx, gx, gyz) <= bound) {
+                baseA = __ldg(S.cell_start + rowbase + xl);
+                nA = __ldg(S.cell_start + rowbase + xl + 1) - baseA;
+              }
+            }
+            if (s > 0 && xr <= b1[0]) {
+              const float gx = axis_gap(xr, q.tx, g.ox, h);
+              if (fmaf(gx, gx, gyz) <= bound) {
+                baseB = __ldg(S.cell_start + rowbase + xr);
+                nB = __ldg(S.cell_start + rowbase + xr + 1) - baseB;
+              }
             }
           }
-          if (xr <= b1[0]) {
-            const float gx = axis_gap(xr, q.tx, g.ox, h);
-            const float bnd2 = EXACT ? band * (1.0f + kRelPrune) : B.d1 * (1.0f + kRelPrune);
-            if (fmaf(gx, gx, gyz) <= bnd2) {
-              const int pb = __ldg(S.cell_start + rowbase + xr), pe = __ldg(S.cell_start + rowbase + xr + 1);
-              scan_range<EXACT>(S.pts, pb, pe, q, B, band, bestD, bestOrig, bestPos);
+        }
+      }
+      const int tot = nA + nB;
+      const int incl = warp_incl_scan(tot);
+      const int excl = incl - tot;
+      const int total = __shfl_sync(kFull, incl, 31);
+      for (int ib = 0; ib < total; ib += 32) {
+        const int i = ib + lane;
+        const int own = warp_owner(incl, i);
+        const int oA = __shfl_sync(kFull, baseA, own), onA = __shfl_sync(kFull, nA, own);
+        const int oB = __shfl_sync(kFull, baseB, own), oe = __shfl_sync(kFull, excl, own);
+        if (i < total) {
+          const int w = i - oe;
+          const int p = (w < onA) ? oA + w : oB + (w - onA);
+          const float4 v = __ldg(S.pts + p);
+          if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+            const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+            const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            if (!EXACT) {
+              if (d < lb1) {
+                lb2 = lb1;
+                lb1 = d;
+                lpos = p;
+                lorig = __float_as_int(v.w);
+              } else if (d < lb2) {
+                lb2 = d;
+              }
+            } else if (d <= band) {
+              const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
+              const int o = __float_as_int(v.w);
+              if (D < lD || (D == lD && o < lDorig)) {
+                lD = D;
+                lDorig = o;
+                lDpos = p;
+              }
             }
           }
         }
       }
     }
+    if (!EXACT) gbest = warp_min(lb1);
   }
 }
 
-// The exact FP64 re-rank runs for a handful of samples per million; keeping it
-// out of line keeps the common path free of its register pressure.
-__device__ __noinline__ int exact_rerank(const SnapDev& S, const BoxQ& q, const CellRange& R, float d1, int* orig) {
-  Best B{d1, d1, -1, -1};
-  const float band = d1 * (1.0f + kRelTie);
-  double bestD = DBL_MAX;
-  int bestOrig = 0x7fffffff, bestPos = -1;
-  ring_pass<true>(S, q, R, B, band, bestD, bestOrig, bestPos);
-  *orig = bestOrig;
-  return bestPos;
-}
-
-// Nearest point strictly inside the box; returns the sorted position (-1 if
-// none) and the original index in *orig.
-__device__ __forceinline__ int nn_search(const SnapDev& S, const BoxQ& q, int* orig) {
+// Nearest point strictly inside the box q (the same for all lanes); the
+// result is returned to every lane.
+__device__ __forceinline__ void coop_search(const SnapDev& S, const BoxQ& q, int* pos, int* orig) {
   const GridParams& g = S.g;
+  *pos = -1;
   *orig = -1;
   if (!(q.lox < g.maxx && q.hix > g.minx && q.loy < g.maxy && q.hiy > g.miny && q.loz < g.maxz &&
         q.hiz > g.minz && q.lox < q.hix && q.loy < q.hiy && q.loz < q.hiz))
-    return -1;
+    return;
   CellRange R;
   R.b0[0] = cell_coord(q.lox, g.ox, g.inv_h, g.dx);
   R.b1[0] = cell_coord(q.hix, g.ox, g.inv_h, g.dx);
@@ -198,21 +255,45 @@ __device__ __forceinline__ int nn_search(const SnapDev& S, const BoxQ& q, int* o
   R.c[0] = cell_coord(q.tx, g.ox, g.inv_h, g.dx);
   R.c[1] = cell_coord(q.ty, g.oy, g.inv_h, g.dy);
   R.c[2] = cell_coord(q.tz, g.oz, g.inv_h, g.dz);
-  Best B{FLT_MAX, FLT_MAX, -1, -1};
-  double bestD = 0.0;
-  int bestOrig = -1, bestPos = -1;
-  ring_pass<false>(S, q, R, B, 0.0f, bestD, bestOrig, bestPos);
-  if (B.pos >= 0 && B.d2 <= B.d1 * (1.0f + kRelTie)) {
-    // possible tie under the FP64 distance: exact re-rank of the contenders
-    return exact_rerank(S, q, R, B.d1, orig);
+  float gbest = FLT_MAX, lb1 = FLT_MAX, lb2 = FLT_MAX;
+  int lpos = -1, lorig = -1, lDorig = 0x7fffffff, lDpos = -1;
+  double lD = DBL_MAX;
+  coop_ring_pass<false>(S, q, R, gbest, 0.0f, lb1, lb2, lpos, lorig, lD, lDorig, lDpos);
+  const float g1 = warp_min(lb1);
+  if (!(g1 < FLT_MAX)) return;
+  const float g2 = warp_min(lb1 == g1 ? lb2 : lb1);
+  if (g2 <= g1 * (1.0f + kRelTie)) {
+    // possible FP64 tie: exact re-rank of the contenders, lowest index wins
+    float fixed = g1;
+    coop_ring_pass<true>(S, q, R, fixed, g1 * (1.0f + kRelTie), lb1, lb2, lpos, lorig, lD, lDorig, lDpos);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double D2 = __shfl_xor_sync(kFull, lD, o);
+      const int o2 = __shfl_xor_sync(kFull, lDorig, o);
+      const int p2 = __shfl_xor_sync(kFull, lDpos, o);
+      if (D2 < lD || (D2 == lD && o2 < lDorig)) {
+        lD = D2;
+        lDorig = o2;
+        lDpos = p2;
+      }
+    }
+    *pos = lDpos;
+    *orig = lDorig;
+  } else {
+    const int w = __ffs(__ballot_sync(kFull, lb1 == g1)) - 1;
+    *pos = __shfl_sync(kFull, lpos, w);
+    *orig = __shfl_sync(kFull, lorig, w);
   }
-  *orig = B.orig;
-  return B.pos;
 }
+
+// ---------------------------------------------------------------------------
+// Rays and segments
+// ---------------------------------------------------------------------------
 
 struct RayCtx {
   int v, i, j;
   double A0, A1, A2, md;
+  float mdf;
   const double3* kt;
 };
 
@@ -256,17 +337,24 @@ __device__ __forceinline__ bool next_ray(const MarchArgs& a, const double3* ktab
     r.A1 = __dadd_rn(__dmul_rn(__dmul_rn(-x, cb), sl), __dmul_rn(y, cl));
     r.A2 = __dmul_rn(-x, sb);
     r.md = V->md;
+    r.mdf = __double2float_rn(V->md);
     r.kt = ktab + (int64_t)v * ktab_stride;
     return true;
   }
 }
 
-// LOS sample k of the ray: exact FP32 target and box (nn:162-179), then NN.
-__device__ __forceinline__ int sample_nn(const SnapDev& S, const RayCtx& r, int k, int* orig) {
+// LOS sample k: derotated position (nn:162-165) in FP64.
+__device__ __forceinline__ void sample_pos(const RayCtx& r, int k, double& p0, double& p1, double& p2) {
   const double3 zt = r.kt[k];
-  const double p0 = __dadd_rn(r.A0, zt.x);
-  const double p1 = __dsub_rn(r.A1, zt.y);
-  const double p2 = __dadd_rn(r.A2, zt.z);
+  p0 = __dadd_rn(r.A0, zt.x);
+  p1 = __dsub_rn(r.A1, zt.y);
+  p2 = __dadd_rn(r.A2, zt.z);
+}
+
+// The reference's FP32 target and box corners of sample k (nn:171-179).
+__device__ __forceinline__ BoxQ exact_box(const RayCtx& r, int k) {
+  double p0, p1, p2;
+  sample_pos(r, k, p0, p1, p2);
   BoxQ q;
   q.tx = __double2float_rn(p0);
   q.ty = __double2float_rn(p1);
@@ -277,7 +365,446 @@ __device__ __forceinline__ int sample_nn(const SnapDev& S, const RayCtx& r, int 
   q.hix = __double2float_rn(__dadd_rn(p0, r.md));
   q.hiy = __double2float_rn(__dadd_rn(p1, r.md));
   q.hiz = __double2float_rn(__dadd_rn(p2, r.md));
-  return nn_search(S, q, orig);
+  return q;
+}
+
+// s-interval of the segment a + s d, s in [slo, shi], whose coordinate lies in [lo, hi].
+__device__ __forceinline__ void clip_interval(float a, float d, float inv_d, float lo, float hi, float& slo,
+                                              float& shi) {
+  if (fabsf(d) > 1e-30f) {
+    const float t1 = (lo - a) * inv_d, t2 = (hi - a) * inv_d;
+    slo = fmaxf(slo, fminf(t1, t2) - 1e-4f);
+    shi = fminf(shi, fmaxf(t1, t2) + 1e-4f);
+  } else if (a < lo || a > hi) {
+    slo = 1.0f;
+    shi = 0.0f;
+  }
+}
+
+// Warp-collective: nearest neighbours of the segment's samples s0 .. s0+63.
+// pos[i]/orig[i] are this lane's results for sample s0 + lane + 32 i.
+__device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r, int s0, int nz, SegSmem& sm,
+                                               int (&pos)[2], int (&orig)[2], unsigned long long* stats) {
+  int st_rows = 0, st_loaded = 0, st_scanned = 0, st_ties = 0, st_samples = 0;
+  const int lane = threadIdx.x & 31;
+  const GridParams& g = S.g;
+  float tx[2], ty[2], tz[2];
+  bool act[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int k = s0 + lane + 32 * i;
+    act[i] = k < nz;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    if (act[i]) sample_pos(r, k, p0, p1, p2);
+    tx[i] = __double2float_rn(p0);  // the FP32 target (nn:171)
+    ty[i] = __double2float_rn(p1);
+    tz[i] = __double2float_rn(p2);
+  }
+  // the segment through the first and last targets
+  const int last = min(s0 + kSeg, nz) - 1;
+  const int nseg = last - s0 + 1;
+  const int li = last - s0, ll = li & 31;
+  const float ax = __shfl_sync(kFull, tx[0], 0), ay = __shfl_sync(kFull, ty[0], 0), az = __shfl_sync(kFull, tz[0], 0);
+  const float bx0 = __shfl_sync(kFull, tx[0], ll), by0 = __shfl_sync(kFull, ty[0], ll),
+              bz0 = __shfl_sync(kFull, tz[0], ll);
+  const float bx1 = __shfl_sync(kFull, tx[1], ll), by1 = __shfl_sync(kFull, ty[1], ll),
+              bz1 = __shfl_sync(kFull, tz[1], ll);
+  const float bx = li >= 32 ? bx1 : bx0, by = li >= 32 ? by1 : by0, bz = li >= 32 ? bz1 : bz0;
+  const float sdx = bx - ax, sdy = by - ay, sdz = bz - az;
+  const float len2 = fmaf(sdz, sdz, fmaf(sdy, sdy, sdx * sdx));
+  const float inv_len2 = len2 > 0.0f ? 1.0f / len2 : 0.0f;
+  const float len = sqrtf(len2);
+  // local point spacing from the occupancy of the cells the segment crosses
+  int occ = 0;
+  {
+    const float fs = (float)lane * (1.0f / 31.0f);
+    const float px = fmaf(fs, sdx, ax), py = fmaf(fs, sdy, ay), pz = fmaf(fs, sdz, az);
+    if (px >= g.minx && px <= g.maxx && py >= g.miny && py <= g.maxy && pz >= g.minz && pz <= g.maxz) {
+      const int c = (cell_coord(pz, g.oz, g.inv_h, g.dz) * g.dy + cell_coord(py, g.oy, g.inv_h, g.dy)) * g.dx +
+                    cell_coord(px, g.ox, g.inv_h, g.dx);
+      occ = __ldg(S.cell_start + c + 1) - __ldg(S.cell_start + c);
+    }
+  }
+  const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
+  const float aloc = g.h * cbrtf(1.0f / mocc);
+  const float R = fminf(r.mdf * 1.7321f * 1.0001f, kRScale * aloc);
+  const float amax =
+      fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
+  const float Rg = R * 1.0001f + amax * 2.4e-7f;  // + a few ulp of the coordinates
+  const float Rg2 = Rg * Rg * (1.0f + kRelPrune);
+  // ---- 1. gather
+  bool gathered = true;
+  int count = 0;
+  const float cxl = fmaxf(fminf(ax, bx) - Rg, g.minx), cxh = fminf(fmaxf(ax, bx) + Rg, g.maxx);
+  const float cyl = fmaxf(fminf(ay, by) - Rg, g.miny), cyh = fminf(fmaxf(ay, by) + Rg, g.maxy);
+  const float czl = fmaxf(fminf(az, bz) - Rg, g.minz), czh = fminf(fmaxf(az, bz) + Rg, g.maxz);
+  if (cxl <= cxh && cyl <= cyh && czl <= czh) {
+    const int x0 = cell_coord(cxl, g.ox, g.inv_h, g.dx), x1 = cell_coord(cxh, g.ox, g.inv_h, g.dx);
+    const int y0 = cell_coord(cyl, g.oy, g.inv_h, g.dy), y1 = cell_coord(cyh, g.oy, g.inv_h, g.dy);
+    const int z0 = cell_coord(czl, g.oz, g.inv_h, g.dz), z1 = cell_coord(czh, g.oz, g.inv_h, g.dz);
+    const int nyr = y1 - y0 + 1, nzr = z1 - z0 + 1;
+    const int nrows = nyr * nzr;
+    st_rows = nrows;
+    if (nrows > kMaxRows) {
+      gathered = false;
+    } else {
+      const float m = kCellMargin * g.h;
+      const float xm = Rg + m + 2e-4f * len;
+      const float inv_dy = fabsf(sdy) > 1e-30f ? 1.0f / sdy : 0.0f;
+      const float inv_dz = fabsf(sdz) > 1e-30f ? 1.0f / sdz : 0.0f;
+      const unsigned lt = (1u << lane) - 1u;
+      for (int rb = 0; rb < nrows; rb += 32) {
+        const int rr = rb + lane;
+        int n = 0, base = 0;
+        if (rr < nrows) {
+          const int jy = y0 + rr % nyr, kz = z0 + rr / nyr;
+          float slo = 0.0f, shi = 1.0f;
+          clip_interval(ay, sdy, inv_dy, fmaf((float)jy, g.h, g.oy) - m - Rg, fmaf((float)(jy + 1), g.h, g.oy) + m + Rg,
+                        slo, shi);
+          clip_interval(az, sdz, inv_dz, fmaf((float)kz, g.h, g.oz) - m - Rg, fmaf((float)(kz + 1), g.h, g.oz) + m + Rg,
+                        slo, shi);
+          slo = fmaxf(slo, 0.0f);
+          shi = fminf(shi, 1.0f);
+          if (slo <= shi) {
+            const float xa = fmaf(slo, sdx, ax), xb = fmaf(shi, sdx, ax);
+            const int c0 = max(x0, cell_coord(fminf(xa, xb) - xm, g.ox, g.inv_h, g.dx));
+            const int c1 = min(x1, cell_coord(fmaxf(xa, xb) + xm, g.ox, g.inv_h, g.dx));
+            if (c0 <= c1) {
+              const int rowbase = (kz * g.dy + jy) * g.dx;
+              base = __ldg(S.cell_start + rowbase + c0);
+              n = __ldg(S.cell_start + rowbase + c1 + 1) - base;
+            }
+          }
+        }
+        // rows' point ranges, prefix-summed across the warp and loaded 32 at a time
+        const int incl = warp_incl_scan(n);
+        const int excl = incl - n;
+        const int total = __shfl_sync(kFull, incl, 31);
+        st_loaded += total;
+        for (int ib = 0; ib < total; ib += 32) {
+          const int i = ib + lane;
+          const int own = warp_owner(incl, i);
+          const int ob = __shfl_sync(kFull, base, own);
+          const int oe = __shfl_sync(kFull, excl, own);
+          bool keep = false;
+          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+          int p = 0, bk = 0;
+          if (i < total) {
+            p = ob + (i - oe);
+            q = __ldg(S.pts + p);
+            const float wx = q.x - ax, wy = q.y - ay, wz = q.z - az;
+            float s = fmaf(wz, sdz, fmaf(wy, sdy, wx * sdx)) * inv_len2;
+            s = fminf(fmaxf(s, 0.0f), 1.0f);
+            const float ex = fmaf(-s, sdx, wx), ey = fmaf(-s, sdy, wy), ez = fmaf(-s, sdz, wz);
+            keep = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= Rg2;
+            bk = min(max(__float2int_rn(s * (float)(nseg - 1)), 0), nseg - 1);
+          }
+          const unsigned msk = __ballot_sync(kFull, keep);
+          if (keep) {
+            const int slot = count + __popc(msk & lt);
+            if (slot < kSegCap) {
+              sm.cq[slot] = q;
+              sm.cpos[slot] = p;
+              sm.cb[slot] = (unsigned char)bk;
+            }
+          }
+          count += __popc(msk);
+        }
+      }
+      if (count > kSegCap) gathered = false;
+    }
+  }
+  const int ncand = gathered ? count : 0;
+  // ---- 2. counting sort by sample index
+  sm.cursor[lane] = 0;
+  sm.cursor[lane + 32] = 0;
+  __syncwarp();
+  for (int c = lane; c < ncand; c += 32) atomicAdd(&sm.cursor[sm.cb[c]], 1);
+  __syncwarp();
+  {
+    const int h0 = sm.cursor[2 * lane], h1 = sm.cursor[2 * lane + 1];
+    const int incl = warp_incl_scan(h0 + h1);
+    const int ex = incl - h0 - h1;
+    __syncwarp();
+    sm.bstart[2 * lane] = ex;
+    sm.bstart[2 * lane + 1] = ex + h0;
+    if (lane == 31) sm.bstart[kSeg] = incl;
+    sm.cursor[2 * lane] = ex;
+    sm.cursor[2 * lane + 1] = ex + h0;
+  }
+  __syncwarp();
+  for (int c = lane; c < ncand; c += 32) {
+    const int dst = atomicAdd(&sm.cursor[sm.cb[c]], 1);
+    sm.sq[dst] = sm.cq[c];
+    sm.spos[dst] = sm.cpos[c];
+  }
+  __syncwarp();
+  // ---- 3./4. per-sample scan of the buckets within R, acceptance
+  const float dlt = (nseg > 1) ? len / (float)(nseg - 1) : 0.0f;
+  const int w = (dlt > 0.0f) ? min((int)(Rg / dlt + 0.51f) + 1, kSeg) : kSeg;
+  pos[0] = pos[1] = -1;
+  orig[0] = orig[1] = -1;
+  bool need0 = false, need1 = false;
+#pragma unroll 1
+  for (int i = 0; i < 2; ++i) {
+    // one copy of the scan code for both samples of the lane (instruction cache)
+    const bool acti = i ? act[1] : act[0];
+    int pres = -1, ores = -1;
+    bool accept = false;
+    if (gathered && acti) {
+      const int j = lane + 32 * i;
+      const int c0 = sm.bstart[max(j - w, 0)], c1 = sm.bstart[min(j + w, nseg - 1) + 1];
+      st_scanned += c1 - c0;
+      const float t_x = i ? tx[1] : tx[0], t_y = i ? ty[1] : ty[0], t_z = i ? tz[1] : tz[0];
+      const float tmax = fmaxf(fmaxf(fabsf(t_x), fabsf(t_y)), fabsf(t_z));
+      const float delta = (tmax + r.mdf) * 4.8e-7f + r.mdf * 1.2e-7f;  // ~4 ulp of the box corners
+      const float md_in = r.mdf - delta, md_out = r.mdf + delta;
+      float b1 = FLT_MAX, b2 = FLT_MAX;
+      int bi = -1;
+      bool amb = false;
+      for (int c = c0; c < c1; ++c) {
+        const float4 q = sm.sq[c];
+        const float dx = q.x - t_x, dy = q.y - t_y, dz = q.z - t_z;
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float cheb = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+        if (cheb < md_in) {
+          if (d2 < b1) {
+            b2 = b1;
+            b1 = d2;
+            bi = c;
+          } else if (d2 < b2) {
+            b2 = d2;
+          }
+        } else if (cheb <= md_out) {
+          amb = true;
+        }
+      }
+      // coverage: every point within cov of the target was gathered
+      const float wx = t_x - ax, wy = t_y - ay, wz = t_z - az;
+      float s = fmaf(wz, sdz, fmaf(wy, sdy, wx * sdx)) * inv_len2;
+      s = fminf(fmaxf(s, 0.0f), 1.0f);
+      const float ex = fmaf(-s, sdx, wx), ey = fmaf(-s, sdy, wy), ez = fmaf(-s, sdz, wz);
+      const float cov = Rg - sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex))) - amax * 2.4e-7f;
+      if (!amb && cov > 0.0f) {
+        if (bi >= 0)
+          accept = b1 < cov * cov * (1.0f - 2.0f * kRelPrune);
+        else
+          accept = md_out * 1.7321f * 1.0001f < cov;  // the whole box lies inside the gathered ball
+      }
+      if (!accept && bi < 0 && !amb) {
+        // no candidate: the box is empty for sure when it lies outside the
+        // points' bounding box (hi <= min or lo >= max on some axis)
+        accept = (t_x + md_out <= g.minx) || (t_x - md_out >= g.maxx) || (t_y + md_out <= g.miny) ||
+                 (t_y - md_out >= g.maxy) || (t_z + md_out <= g.minz) || (t_z - md_out >= g.maxz);
+      }
+      if (accept && bi >= 0) {
+        if (b2 <= b1 * (1.0f + kRelTie)) {
+          // possible FP64 tie: exact re-rank of the in-box contenders
+          ++st_ties;
+          const float band = b1 * (1.0f + kRelTie);
+          double bestD = DBL_MAX;
+          int bestOrig = 0x7fffffff;
+          for (int c = c0; c < c1; ++c) {
+            const float4 q = sm.sq[c];
+            const float dx = q.x - t_x, dy = q.y - t_y, dz = q.z - t_z;
+            const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float cheb = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+            if (cheb < md_in && d2 <= band) {
+              const double D = exact_dist2(q.x, q.y, q.z, t_x, t_y, t_z);
+              const int o = __float_as_int(q.w);
+              if (D < bestD || (D == bestD && o < bestOrig)) {
+                bestD = D;
+                bestOrig = o;
+                bi = c;
+              }
+            }
+          }
+        }
+        pres = sm.spos[bi];
+        ores = __float_as_int(sm.sq[bi].w);
+      }
+    }
+    st_samples += acti ? 1 : 0;
+    const bool need = acti && !accept;
+    if (i) {
+      pos[1] = pres;
+      orig[1] = ores;
+      need1 = need;
+    } else {
+      pos[0] = pres;
+      orig[0] = ores;
+      need0 = need;
+    }
+  }
+  __syncwarp();  // the candidate lists are reused below and by the next segment
+  // ---- 5. the remaining samples: gather the points of the union of their
+  // boxes once, then every such sample scans that list with its exact box
+  const unsigned f0 = __ballot_sync(kFull, need0), f1 = __ballot_sync(kFull, need1);
+  if (f0 | f1) {
+    float ulx = FLT_MAX, uly = FLT_MAX, ulz = FLT_MAX, uhx = -FLT_MAX, uhy = -FLT_MAX, uhz = -FLT_MAX;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      if (i ? need1 : need0) {
+        const float t_x = i ? tx[1] : tx[0], t_y = i ? ty[1] : ty[0], t_z = i ? tz[1] : tz[0];
+        const float tmax = fmaxf(fmaxf(fabsf(t_x), fabsf(t_y)), fabsf(t_z));
+        const float mo = r.mdf + (tmax + r.mdf) * 4.8e-7f + r.mdf * 1.2e-7f;  // superset of the exact box
+        ulx = fminf(ulx, t_x - mo);
+        uly = fminf(uly, t_y - mo);
+        ulz = fminf(ulz, t_z - mo);
+        uhx = fmaxf(uhx, t_x + mo);
+        uhy = fmaxf(uhy, t_y + mo);
+        uhz = fmaxf(uhz, t_z + mo);
+      }
+    }
+    ulx = fmaxf(warp_min(ulx), g.minx);
+    uly = fmaxf(warp_min(uly), g.miny);
+    ulz = fmaxf(warp_min(ulz), g.minz);
+    uhx = fminf(-warp_min(-uhx), g.maxx);
+    uhy = fminf(-warp_min(-uhy), g.maxy);
+    uhz = fminf(-warp_min(-uhz), g.maxz);
+    bool ok = true;
+    int ucount = 0;
+    if (ulx <= uhx && uly <= uhy && ulz <= uhz) {
+      const int x0 = cell_coord(ulx, g.ox, g.inv_h, g.dx), x1 = cell_coord(uhx, g.ox, g.inv_h, g.dx);
+      const int y0 = cell_coord(uly, g.oy, g.inv_h, g.dy), y1 = cell_coord(uhy, g.oy, g.inv_h, g.dy);
+      const int z0 = cell_coord(ulz, g.oz, g.inv_h, g.dz), z1 = cell_coord(uhz, g.oz, g.inv_h, g.dz);
+      const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
+      const unsigned lt = (1u << lane) - 1u;
+      if (nrows > kMaxRows) ok = false;
+      for (int rb = 0; ok && rb < nrows; rb += 32) {
+        const int rr = rb + lane;
+        int n = 0, base = 0;
+        if (rr < nrows) {
+          const int rowbase = ((z0 + rr / nyr) * g.dy + (y0 + rr % nyr)) * g.dx;
+          base = __ldg(S.cell_start + rowbase + x0);
+          n = __ldg(S.cell_start + rowbase + x1 + 1) - base;
+        }
+        const int incl = warp_incl_scan(n);
+        const int excl = incl - n;
+        const int total = __shfl_sync(kFull, incl, 31);
+        for (int ib = 0; ib < total; ib += 32) {
+          const int i = ib + lane;
+          const int own = warp_owner(incl, i);
+          const int ob = __shfl_sync(kFull, base, own);
+          const int oe = __shfl_sync(kFull, excl, own);
+          bool keep = false;
+          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+          int p = 0;
+          if (i < total) {
+            p = ob + (i - oe);
+            q = __ldg(S.pts + p);
+            keep = q.x >= ulx && q.x <= uhx && q.y >= uly && q.y <= uhy && q.z >= ulz && q.z <= uhz;
+          }
+          const unsigned msk = __ballot_sync(kFull, keep);
+          if (keep) {
+            const int slot = ucount + __popc(msk & lt);
+            if (slot < kSegCap) {
+              sm.sq[slot] = q;
+              sm.spos[slot] = p;
+            }
+          }
+          ucount += __popc(msk);
+        }
+      }
+      if (ucount > kSegCap) ok = false;
+    }
+    __syncwarp();
+    if (ok) {
+#pragma unroll 1
+      for (int i = 0; i < 2; ++i) {
+        if (i ? need1 : need0) {
+          const BoxQ q = exact_box(r, s0 + lane + 32 * i);
+          float b1 = FLT_MAX, b2 = FLT_MAX;
+          int bi = -1;
+          for (int c = 0; c < ucount; ++c) {
+            const float4 v = sm.sq[c];
+            if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+              const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+              const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              if (d2 < b1) {
+                b2 = b1;
+                b1 = d2;
+                bi = c;
+              } else if (d2 < b2) {
+                b2 = d2;
+              }
+            }
+          }
+          if (bi >= 0 && b2 <= b1 * (1.0f + kRelTie)) {
+            // possible FP64 tie: exact re-rank, lowest original index wins
+            const float band = b1 * (1.0f + kRelTie);
+            double bestD = DBL_MAX;
+            int bestOrig = 0x7fffffff;
+            for (int c = 0; c < ucount; ++c) {
+              const float4 v = sm.sq[c];
+              if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+                const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+                if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= band) {
+                  const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
+                  const int o = __float_as_int(v.w);
+                  if (D < bestD || (D == bestD && o < bestOrig)) {
+                    bestD = D;
+                    bestOrig = o;
+                    bi = c;
+                  }
+                }
+              }
+            }
+          }
+          const int pres = bi >= 0 ? sm.spos[bi] : -1;
+          const int ores = bi >= 0 ? __float_as_int(sm.sq[bi].w) : -1;
+          if (i) {
+            pos[1] = pres;
+            orig[1] = ores;
+          } else {
+            pos[0] = pres;
+            orig[0] = ores;
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (!ok) {
+  // ---- 6. overflow: the remaining samples one at a time, by the whole warp
+#pragma unroll 1
+  for (int i = 0; i < 2; ++i) {
+    unsigned fm = i ? f1 : f0;
+    while (fm) {
+      const int sl = __ffs(fm) - 1;
+      fm &= fm - 1;
+      const BoxQ q = exact_box(r, s0 + sl + 32 * i);
+      int p, o;
+      coop_search(S, q, &p, &o);
+      if (lane == sl) {
+        if (i) {
+          pos[1] = p;
+          orig[1] = o;
+        } else {
+          pos[0] = p;
+          orig[0] = o;
+        }
+      }
+    }
+  }
+    }
+  }
+  __syncwarp();  // the lists are rewritten by the next segment
+  if (stats) {
+    const unsigned sc = __reduce_add_sync(kFull, (unsigned)st_scanned);
+    const unsigned ti = __reduce_add_sync(kFull, (unsigned)st_ties);
+    const unsigned sa = __reduce_add_sync(kFull, (unsigned)st_samples);
+    if (lane == 0) {
+      atomicAdd(stats + kStatSegments, 1ull);
+      atomicAdd(stats + kStatCandidates, (unsigned long long)count);
+      atomicAdd(stats + kStatRows, (unsigned long long)st_rows);
+      atomicAdd(stats + kStatPointsLoaded, (unsigned long long)st_loaded);
+      atomicAdd(stats + kStatNotGathered, gathered ? 0ull : 1ull);
+      atomicAdd(stats + kStatFallbacks, (unsigned long long)(__popc(f0) + __popc(f1)));
+      atomicAdd(stats + kStatSamples, (unsigned long long)sa);
+      atomicAdd(stats + kStatScanned, (unsigned long long)sc);
+      atomicAdd(stats + kStatTies, (unsigned long long)ti);
+    }
+  }
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -287,11 +814,14 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // ---------------------------------------------------------------------------
-// Spectroscopic march: NL lines x NB bins per lane (bin = m*32 + lane).
+// Spectroscopic march: NL lines x up to NB 32-bin windows per line; lane
+// `lane` owns bins wstart + 32 m + lane of each line.
 // ---------------------------------------------------------------------------
 template <int NL, int NB>
 __global__ void __launch_bounds__(kThreads) march_spectral(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride) {
+  __shared__ SegSmem segs[kWarps];
+  SegSmem& sm = segs[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   RayCtx r;
   while (next_ray(a, ktab, ktab_stride, r)) {
@@ -299,62 +829,100 @@ __global__ void __launch_bounds__(kThreads) march_spectral(MarchArgs a, const do
     const int nz = V->nz, L = V->L, nx = V->nx;
     const float ux = V->ux, uy = V->uy, uz = V->uz;
     const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
-    float acc[NL][NB], comp[NL][NB], lam[NL][NB], shk[NL];
+    float acc[NL][NB], comp[NL][NB], part[NL][NB], lam[NL][NB], shk[NL];
     const float2* ew[NL];
     bool lon[NL];
+    int nw[NL], ws[NL];
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
       const bool on = l < a.nlines && LD[l].ew != nullptr;  // views may have fewer lines than the launch
       lon[l] = on;
       ew[l] = on ? LD[l].ew : nullptr;
       shk[l] = on ? LD[l].shift_k : 0.0f;
+      nw[l] = on ? min(LD[l].nw, NB) : 0;
+      ws[l] = on ? LD[l].wstart : 0;
 #pragma unroll
       for (int m = 0; m < NB; ++m) {
-        const int il = m * 32 + lane;
+        const int il = ws[l] + m * 32 + lane;
         acc[l][m] = 0.0f;
         comp[l][m] = 0.0f;
+        part[l][m] = 0.0f;
         // lambdaval (nn:200), evaluated in FP64 on the host, stored FP32
-        lam[l][m] = (on && il < L) ? __ldg(LD[l].lam + il) : 3.0e30f;
+        lam[l][m] = (m < nw[l] && il < L) ? __ldg(LD[l].lam + il) : 3.0e30f;
       }
     }
     int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
     const int64_t ray = (int64_t)r.i * nx + r.j;
-    for (int k0 = 0; k0 < nz; k0 += 32) {
-      const int k = k0 + lane;
-      const bool active = k < nz;
-      int orig = -1;
-      const int pos = active ? sample_nn(a.snap, r, k, &orig) : -1;
-      if (nnout && active) nnout[ray * nz + k] = orig;
-      const int prev = __shfl_up_sync(kFull, pos, 1);
-      const bool start = active && (lane == 0 || pos != prev);
-      unsigned starts = __ballot_sync(kFull, start);
-      const unsigned act = __ballot_sync(kFull, active);
-      const int endlane = 32 - __clz(act);
-      while (starts) {
-        const int s = __ffs(starts) - 1;
-        starts &= starts - 1;
-        const int e = starts ? (__ffs(starts) - 1) : endlane;
-        const int id = __shfl_sync(kFull, pos, s);
-        if (id < 0) continue;
-        const float cnt = (float)(e - s);
-        const float4 vv = __ldg(a.snap.vel + id);
-        const float vlos = fmaf(uz, vv.z, fmaf(uy, vv.y, ux * vv.x));
+    for (int s0 = 0; s0 < nz; s0 += kSeg) {
+      int posv[2], origv[2];
+      segment_search(a.snap, r, s0, nz, sm, posv, origv, a.stats);
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        const int k = s0 + 32 * h + lane;
+        const bool active = k < nz;
+        const int pos = h ? posv[1] : posv[0];
+        if (nnout && active) nnout[ray * nz + k] = h ? origv[1] : origv[0];
+        // runs of equal neighbours
+        const int prev = __shfl_up_sync(kFull, pos, 1);
+        const bool start = active && (lane == 0 || pos != prev);
+        const unsigned starts = __ballot_sync(kFull, start);
+        const unsigned act = __ballot_sync(kFull, active);
+        if (!act) break;
+        const int endlane = 32 - __clz(act);
+        // the start lane of each run loads its payload and forms the per-line terms
+        float rpk[NL], rsc[NL], rns[NL];
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
-          if (lon[l]) {
-            const float2 pw = __ldg(ew[l] + id);
-            if (pw.x != 0.0f) {
-              const float pk = pw.x * cnt;
-              const float sc = __fdividef(2.0f, pw.y);  // exp(-4 ln2 (d/w)^2) = 2^(-(2d/w)^2)
-              const float sh = vlos * shk[l];
+          rpk[l] = 0.0f;
+          rsc[l] = 0.0f;
+          rns[l] = 0.0f;
+        }
+        if (start && pos >= 0) {
+          const unsigned later = starts & ~((2u << lane) - 1u);
+          const int e = later ? (__ffs(later) - 1) : endlane;
+          const float cnt = (float)(e - lane);
+          const float4 vv = __ldg(a.snap.vel + pos);
+          const float vlos = fmaf(uz, vv.z, fmaf(uy, vv.y, ux * vv.x));
 #pragma unroll
-              for (int m = 0; m < NB; ++m) {
-                const float q = (lam[l][m] - sh) * sc;
-                kahan_add(acc[l][m], comp[l][m], pk * ex2_approx(-q * q));
+          for (int l = 0; l < NL; ++l) {
+            if (lon[l]) {
+              const float2 pw = __ldg(ew[l] + pos);
+              const float sc = __fdividef(2.0f, pw.y);  // exp(-4 ln2 (d/w)^2) = 2^(-(2d/w)^2)
+              rpk[l] = pw.x * cnt;
+              rsc[l] = sc;
+              rns[l] = -(vlos * shk[l]) * sc;
+            }
+          }
+        }
+        unsigned todo = starts;
+        while (todo) {
+          const int s = __ffs(todo) - 1;
+          todo &= todo - 1;
+#pragma unroll
+          for (int l = 0; l < NL; ++l) {
+            if (lon[l]) {
+              const float pk = __shfl_sync(kFull, rpk[l], s);
+              if (pk != 0.0f) {  // intpolpeak ? ... : 0 (nn:204); no neighbour -> 0
+                const float sc = __shfl_sync(kFull, rsc[l], s);
+                const float ns = __shfl_sync(kFull, rns[l], s);
+#pragma unroll
+                for (int m = 0; m < NB; ++m) {
+                  if (m < nw[l]) {
+                    const float q = fmaf(lam[l][m], sc, ns);
+                    part[l][m] = fmaf(pk, ex2_approx(-q * q), part[l][m]);
+                  }
+                }
               }
             }
           }
         }
+#pragma unroll
+        for (int l = 0; l < NL; ++l)
+#pragma unroll
+          for (int m = 0; m < NB; ++m) {
+            kahan_add(acc[l][m], comp[l][m], part[l][m]);
+            part[l][m] = 0.0f;
+          }
       }
     }
 #pragma unroll
@@ -362,10 +930,13 @@ __global__ void __launch_bounds__(kThreads) march_spectral(MarchArgs a, const do
       if (lon[l]) {
         const double scale = LD[l].is_dn ? V->scale_dn : V->scale;
         float* out = LD[l].out + ray * L;
+        const int wlo = ws[l], whi = ws[l] + 32 * nw[l];
+        for (int il = lane; il < L; il += 32)
+          if (il < wlo || il >= whi) out[il] = 0.0f;  // below 2^-64 of every peak
 #pragma unroll
         for (int m = 0; m < NB; ++m) {
-          const int il = m * 32 + lane;
-          if (il < L) out[il] = __double2float_rn(__dmul_rn(scale, (double)acc[l][m]));
+          const int il = wlo + m * 32 + lane;
+          if (m < nw[l] && il < L) out[il] = __double2float_rn(__dmul_rn(scale, (double)acc[l][m]));
         }
       }
     }
@@ -379,6 +950,8 @@ __global__ void __launch_bounds__(kThreads) march_spectral(MarchArgs a, const do
 template <int NL, bool THOMSON>
 __global__ void __launch_bounds__(kThreads) march_imaging(MarchArgs a, const double3* __restrict__ ktab,
                                                           int ktab_stride) {
+  __shared__ SegSmem segs[kWarps];
+  SegSmem& sm = segs[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   RayCtx r;
   while (next_ray(a, ktab, ktab_stride, r)) {
@@ -396,26 +969,30 @@ __global__ void __launch_bounds__(kThreads) march_imaging(MarchArgs a, const dou
     const float* s2v = THOMSON ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
     int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
     const int64_t ray = (int64_t)r.i * nx + r.j;
-    for (int k0 = 0; k0 < nz; k0 += 32) {
-      const int k = k0 + lane;
-      const bool active = k < nz;
-      int orig = -1;
-      const int pos = active ? sample_nn(a.snap, r, k, &orig) : -1;
-      if (nnout && active) nnout[ray * nz + k] = orig;
+    for (int s0 = 0; s0 < nz; s0 += kSeg) {
+      int posv[2], origv[2];
+      segment_search(a.snap, r, s0, nz, sm, posv, origv, a.stats);
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        const int k = s0 + 32 * h + lane;
+        const bool active = k < nz;
+        const int pos = h ? posv[1] : posv[0];
+        if (nnout && active) nnout[ray * nz + k] = h ? origv[1] : origv[0];
 #pragma unroll
-      for (int l = 0; l < NL; ++l) {
-        if (lon[l]) {
-          float val = 0.0f;
-          if (pos >= 0) {
-            if (THOMSON) {
-              // pB = pol * sin^2 chi, clamped at 0 (thomson:325-338)
-              val = fmaxf(__ldg(a.totpol + pos).y * __ldg(s2v + pos), 0.0f);
-            } else {
-              val = __ldg(LD[l].ew + pos).x;  // imaging adds the peak (nn:217-225)
+        for (int l = 0; l < NL; ++l) {
+          if (lon[l]) {
+            float val = 0.0f;
+            if (pos >= 0) {
+              if (THOMSON) {
+                // pB = pol * sin^2 chi, clamped at 0 (thomson:325-338)
+                val = fmaxf(__ldg(a.totpol + pos).y * __ldg(s2v + pos), 0.0f);
+              } else {
+                val = __ldg(LD[l].ew + pos).x;  // imaging adds the peak (nn:217-225)
+              }
             }
+            const float cs = warp_sum(val);
+            if (lane == 0) kahan_add(acc[l], comp[l], cs);
           }
-          const float cs = warp_sum(val);
-          if (lane == 0) kahan_add(acc[l], comp[l], cs);
         }
       }
     }
@@ -436,9 +1013,8 @@ cudaError_t launch_persistent(K kernel, const MarchArgs& a, const double3* ktab,
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   if (blocks_per_sm_hint > 0 && blocks_per_sm_hint < per_sm) per_sm = blocks_per_sm_hint;
-  int64_t warps_needed = a.total_items;
   int64_t blocks = (int64_t)sm_count * per_sm;
-  const int64_t cap = (warps_needed + (kThreads / 32) - 1) / (kThreads / 32);
+  const int64_t cap = (a.total_items + kWarps - 1) / kWarps;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   kernel<<<(unsigned)blocks, kThreads, 0, s>>>(a, ktab, ktab_stride);
@@ -452,24 +1028,26 @@ int march_bins_per_lane(int nlines, int L) {
   return (L + 31) / 32;
 }
 
-cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_L, int sm_count,
-                         cudaStream_t s, int blocks_per_sm_hint) {
+// max_windows: largest number of 32-bin lambda windows of any line (1 for imaging).
+cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
+                         cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
   const bool thomson = a.s2 != nullptr;
   if (thomson) return launch_persistent(march_imaging<1, true>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
-  if (max_L <= 1) {
+  if (imaging) {
     if (a.nlines <= 1) return launch_persistent(march_imaging<1, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
     if (a.nlines <= 2) return launch_persistent(march_imaging<2, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
     if (a.nlines <= 4) return launch_persistent(march_imaging<4, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
     if (a.nlines <= 8) return launch_persistent(march_imaging<8, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
     return cudaErrorInvalidValue;
   }
-  const int nb = (max_L + 31) / 32;
+  const int nb = max_windows < 1 ? 1 : max_windows;
 #define FOMO_SPEC(NL_, NB_) \
   if (a.nlines <= NL_ && nb <= NB_) return launch_persistent(march_spectral<NL_, NB_>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint)
   FOMO_SPEC(1, 1);
   FOMO_SPEC(1, 2);
   FOMO_SPEC(1, 4);
   FOMO_SPEC(1, 8);
+  FOMO_SPEC(2, 1);
   FOMO_SPEC(2, 2);
   FOMO_SPEC(2, 4);
   FOMO_SPEC(4, 1);

@@ -344,7 +344,11 @@ int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec
     e = launch_scatter(a[0], a[1], a[2], a[5], a[6], a[7], a[3], a[4], n, cell_of, R.cell_start, fill, R.pts, R.vel,
                        R.ne, R.T, s);
   if (e == cudaSuccess) e = launch_sort_cells(R.cell_start, ncells, R.pts, R.vel, R.ne, R.T, s);
+  unsigned int vbits = 0x7f800000u;
+  if (e == cudaSuccess) e = launch_speed_max(R.vel, n, bits, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&vbits, bits, sizeof(vbits), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  std::memcpy(&R.vmax, &vbits, sizeof(R.vmax));
   dev_free(ctx, stage);
   dev_free(ctx, bits);
   dev_free(ctx, tmp);
@@ -400,13 +404,46 @@ int get_payload(fomo_ctx* ctx, int snap, int table, int imaging, double abund, c
   td.imaging = imaging;
   cudaError_t e = launch_emission(sit->second.ne, sit->second.T, sit->second.n, td, static_cast<float2*>(p),
                                   ctx->stream);
+  // largest line width of the emitting points: bounds the evaluated lambda window
+  unsigned int* wb = reinterpret_cast<unsigned int*>(ctx->stats_dev);
+  unsigned int hw = 0x7f800000u;
+  if (e == cudaSuccess) e = launch_payload_stats(static_cast<float2*>(p), sit->second.n, wb, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hw, wb, sizeof(hw), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     dev_free(ctx, p);
     return cuda_err(ctx, e, "emission kernel");
   }
+  float wmax;
+  std::memcpy(&wmax, &hw, sizeof(wmax));
   ctx->payloads[key] = static_cast<float2*>(p);
+  ctx->payload_wmax[key] = imaging ? 1.0f : wmax;
   *out = static_cast<float2*>(p);
   return FOMO_OK;
+}
+
+float payload_wmax(fomo_ctx* ctx, int snap, int table, int imaging, double abund) {
+  auto it = ctx->payload_wmax.find(std::make_tuple(snap, table, imaging, abund));
+  return it == ctx->payload_wmax.end() ? __builtin_inff() : it->second;
+}
+
+// lambda window of one line: bins whose Gaussian weight is below 2^-64 of every
+// peak (|dlambda| > 4 w_max beyond the largest Doppler shift) are not evaluated.
+void line_window(double lwa, int L, double lambda0, float vmax, float wmax, int* wstart, int* nw) {
+  const int full = (L + 31) / 32;
+  *wstart = 0;
+  *nw = full;
+  if (L <= 1 || !(lwa > 0) || !std::isfinite(wmax) || !std::isfinite(vmax)) return;
+  const double dl = lwa / (L - 1);
+  const double S = ((double)vmax * lambda0 / FOMO_SPEED_OF_LIGHT + 4.0 * (double)wmax) * 1.001 + 2.0 * dl;
+  const double lo = (lwa / 2. - S) / dl, hi = (lwa / 2. + S) / dl;
+  int b0 = (int)std::floor(std::max(lo, 0.0));
+  int b1 = (int)std::ceil(std::min(hi, (double)(L - 1)));
+  if (b1 < b0) b1 = b0;
+  const int n = (b1 - b0 + 1 + 31) / 32;
+  if (n >= full) return;
+  *wstart = b0;
+  *nw = n;
 }
 
 int get_thomson_payload(fomo_ctx* ctx, SnapRec& r, const float2** out) {
@@ -684,6 +721,8 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
           LD.lwa = q.lambda_width * t.lambda0 / FOMO_SPEED_OF_LIGHT;  // nn:116
           LD.shift_k = (float)(t.lambda0 / FOMO_SPEED_OF_LIGHT);
           LD.is_dn = t.is_dn ? 1 : 0;
+          line_window(LD.lwa, q.nlambda, t.lambda0, ctx->snaps[G.snapshot].vmax,
+                      payload_wmax(ctx, G.snapshot, q.table, G.imaging, q.abundratio), &LD.wstart, &LD.nw);
           const int Lq = q.nlambda;
           float* lam = hlam + lam_pos;
           for (int il = 0; il < Lq && Lq > 1; ++il)
@@ -702,6 +741,9 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
       }
     }
     G.total_items = hoff[G.nv];
+    G.max_nw = 1;
+    for (int v = 0; v < G.nv; ++v)
+      for (int li = 0; li < (int)G.vreqs[v].size(); ++li) G.max_nw = std::max(G.max_nw, hl[(size_t)v * G.nl + li].nw);
     G.vbase = vbase;
     vbase += G.nv;
   }
@@ -714,8 +756,17 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
 // view set-up and the persistent march.
 int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s) {
   char* db = scr->arena.base;
+  // Under stream capture an ordinary event record is only a capture-internal
+  // dependency: the staging event is then recorded after the graph launch,
+  // and the timing events become external event-record nodes.
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  const bool capturing = cs == cudaStreamCaptureStatusActive;
+  auto record_timing = [&](cudaEvent_t ev) {
+    return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal) : cudaEventRecord(ev, s);
+  };
   cudaError_t e = cudaMemcpyAsync(db, scr->staging.base, plan.host_bytes, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && scr->staging.copy_done) e = cudaEventRecord(scr->staging.copy_done, s);
+  if (e == cudaSuccess && scr->staging.copy_done && !capturing) e = cudaEventRecord(scr->staging.copy_done, s);
   for (const PlanGroup& G : plan.groups) {
     if (e != cudaSuccess) break;
     SnapRec& snap = ctx->snaps[G.snapshot];
@@ -740,10 +791,12 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s)
     a.nn_idx = G.any_nn ? reinterpret_cast<int32_t* const*>(db + G.o_nnp) : nullptr;
     a.s2 = s2;
     a.totpol = G.totpol;
-    if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = cudaEventRecord(scr->ev0, s);
+    a.stats = ctx->march_stats;
+    if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = record_timing(scr->ev0);
     if (e == cudaSuccess)
-      e = launch_march(a, ktab, G.maxnz, G.method == FOMO_METHOD_THOMSON ? 1 : G.maxL, ctx->sm_count, s, G.bps);
-    if (e == cudaSuccess && scr->ev1 && ctx->time_march) e = cudaEventRecord(scr->ev1, s);
+      e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
+                       G.method == FOMO_METHOD_THOMSON || G.imaging);
+    if (e == cudaSuccess && scr->ev1 && ctx->time_march) e = record_timing(scr->ev1);
   }
   if (e != cudaSuccess) return cuda_err(ctx, e, "render launch");
   return FOMO_OK;
@@ -822,12 +875,16 @@ int fomo_ctx_create(int device, size_t hbm_budget_bytes, fomo_ctx** out) {
   cudaMemGetInfo(&fr, &tot);
   ctx->budget = hbm_budget_bytes ? hbm_budget_bytes : (size_t)(0.9 * (double)fr);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      ctx->scratch.init() != cudaSuccess ||
+      ctx->scratch.init() != cudaSuccess || cudaMalloc(&ctx->stats_dev, 256) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->order_ev, cudaEventDisableTiming) != cudaSuccess) {
     delete ctx;
     return FOMO_EDEVICE;
   }
   if (const char* tc = std::getenv("FOMO_TUNE_CACHE")) load_tune_cache(ctx, tc);
+  if (const char* ms = std::getenv("FOMO_MARCH_STATS")) {
+    if (ms[0] == '1' && cudaMalloc(&ctx->march_stats, sizeof(unsigned long long) * kStatCount) == cudaSuccess)
+      cudaMemset(ctx->march_stats, 0, sizeof(unsigned long long) * kStatCount);
+  }
   const char* tm = std::getenv("FOMO_TIME_MARCH");
   ctx->time_march = !(tm && tm[0] == '0');
   *out = ctx;
@@ -849,6 +906,17 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
   for (auto& kv : ctx->tables) dev_free(ctx, kv.second.d);
   dev_free(ctx, ctx->scratch.arena.base);
   dev_free(ctx, ctx->out_arena.base);
+  if (ctx->stats_dev) cudaFree(ctx->stats_dev);
+  if (ctx->march_stats) {
+    unsigned long long h[kStatCount] = {0};
+    cudaMemcpy(h, ctx->march_stats, sizeof(h), cudaMemcpyDeviceToHost);
+    std::fprintf(stderr,
+                 "fomo march stats: segments %llu candidates %llu rows %llu points_loaded %llu not_gathered %llu "
+                 "fallbacks %llu samples %llu scanned %llu ties %llu\n",
+                 h[kStatSegments], h[kStatCandidates], h[kStatRows], h[kStatPointsLoaded], h[kStatNotGathered],
+                 h[kStatFallbacks], h[kStatSamples], h[kStatScanned], h[kStatTies]);
+    cudaFree(ctx->march_stats);
+  }
   ctx->scratch.release();
   cudaEventDestroy(ctx->order_ev);
   cudaStreamDestroy(ctx->stream);

@@ -38,6 +38,7 @@ struct SnapRec {
   float* T = nullptr;
   int* cell_start = nullptr;
   float2* totpol = nullptr;  // Thomson payload, built on first use
+  float vmax = 0.0f;         // largest |v| (bounds every Doppler shift)
 };
 
 // Grow-only device scratch; contents belong to the work last enqueued.
@@ -86,6 +87,7 @@ struct PlanGroup {
   std::vector<int> reqs;
   std::vector<std::vector<int>> vreqs;  // requests (lines) of each view
   int nv = 0, nl = 1, maxL = 1, maxnz = 1, maxnx = 2, maxny = 2;
+  int max_nw = 1;  // largest number of 32-bin lambda windows of a line
   int tw = 8, th = 4, bps = 0;
   std::vector<const float2*> ew;       // payload per request (NN)
   const float2* totpol = nullptr;      // Thomson payload
@@ -131,6 +133,9 @@ struct fomo_ctx {
   std::map<int, fomo::SnapRec> snaps;
   std::map<int, fomo::TableRec> tables;
   std::map<std::tuple<int, int, int, double>, float2*> payloads;
+  std::map<std::tuple<int, int, int, double>, float> payload_wmax;  // largest FWHM of emitting points
+  void* stats_dev = nullptr;  // small device buffer for reductions read back by the host
+  unsigned long long* march_stats = nullptr;  // search counters (FOMO_MARCH_STATS=1), printed at destroy
   fomo::ScratchSet scratch;  // descriptors, per-view tables, Thomson sin^2 chi
   fomo::Arena out_arena;     // device cubes of host-output renders
   std::vector<fomo::ViewReadback> view_readback;
