@@ -95,6 +95,7 @@ SIGNATURES = {
     "fomo_render": [ctypes.c_void_p, ctypes.POINTER(Request), _F, _I32, ctypes.POINTER(ViewInfo)],
     "fomo_render_device": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_void_p, ctypes.c_void_p,
                            ctypes.POINTER(ViewInfo), ctypes.c_void_p],
+    "fomo_render_noalloc": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_void_p, ctypes.c_void_p],
     "fomo_render_batch": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_int, ctypes.POINTER(_F),
                           ctypes.POINTER(ViewInfo)],
     "fomo_render_batch_device": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_int,

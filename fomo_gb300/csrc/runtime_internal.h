@@ -163,6 +163,10 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
 int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s);
 std::string workload_class(const PlanGroup& G, const SnapRec& snap);
 int order_streams(fomo_ctx* ctx, cudaStream_t s);
+SnapDev snap_dev(const SnapRec& r);
+float payload_wmax(fomo_ctx* ctx, int snap, int table, int imaging, double abund);
+void line_window(double lwa, int L, double lambda0, float vmax, float wmax, int* wstart, int* nw);
+void fill_view_host(const fomo_request& q, double lambda0, int tw, int th, ViewDesc* V);
 int finish_views(fomo_ctx* ctx, std::vector<ViewDesc>* views);
 void view_info_from(const ViewDesc& V, const fomo_request& q, const TableHost* t, fomo_view_info* info);
 int parse_table_text(const std::string& text, TableHost* t, std::string* err);

@@ -157,6 +157,22 @@ int fomo_render(fomo_ctx* ctx, const fomo_request* req, float* out_cube, int32_t
 int fomo_render_device(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube, int32_t* d_out_nn_idx,
                        fomo_view_info* info, void* stream);
 
+/* Render one NearestNeighbour request into a caller device buffer WITHOUT
+ * allocating anything.  No counterpart in the reference: it exists for callers
+ * that must not allocate device memory while they render (an application
+ * that owns a fixed device-memory pool and forbids allocation in its frame
+ * loop, or a real-time path where cudaMalloc/cudaFree would synchronise the
+ * device).  The per-render working memory lives in one static device array of
+ * about 167 KB that every GPU loading this library holds until exit; hence the
+ * limits nz <= 4096, nx + ny <= 8192, nlambda <= 256 (larger requests return
+ * FOMO_EINVAL).  The snapshot, the table and the emissivity of the pair must
+ * already be resident (call fomo_emission or any regular render once first).
+ * The first call on a device looks up the array's address, so make it before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (different streams) race and must be serialised.  Asynchronous on
+ * `stream` (NULL = the context's stream). */
+int fomo_render_noalloc(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube, void* stream);
+
 /* Batched render: many views / lines / requests in one persistent launch.
  * Requests that share snapshot, method, angles and resolution share their
  * neighbour lookups (one lookup per LOS sample feeds every line).  outs[r]

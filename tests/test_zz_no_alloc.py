@@ -1,0 +1,49 @@
+"""fomo_render_noalloc: the render entry point for callers that must not
+allocate device memory while they render (their working memory is a fixed
+static device array inside the library).  Its cube must match the regular
+render's, call after call.  Collected last on purpose (file name), so a run
+that stops at the first failure has run every other test before it."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import fomo_gb300 as fg
+from fomo_gb300 import synth
+from tests import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4  # normalised max error, as for every other render test
+
+
+def test_noalloc_render_matches_regular_render_on_consecutive_calls():
+    import torch
+
+    with fg.Context(0) as ctx:
+        lib = fg.lib()
+        s = synth.loop_snapshot(24, seed=21)
+        t = synth.line_table()
+        sid = ctx.snapshot(s)
+        tid = ctx.table(t)
+        width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+        req = ctx.request(sid, tid, fg.METHOD_NN, 40, 36, 96, 64, 0.7, -0.35, width)
+        # the regular entry point; it also makes this snapshot/table emissivity resident
+        ref, _, _ = ctx.render(req)
+        out = torch.empty(ref.shape, dtype=torch.float32, device="cuda:0")
+        for _ in range(2):
+            out.fill_(float("nan"))
+            torch.cuda.synchronize()
+            rc = lib.fomo_render_noalloc(ctx.h, ctypes.byref(req), ctypes.c_void_p(out.data_ptr()), None)
+            assert rc == fg.OK, lib.fomo_last_error(ctx.h).decode()
+            ctx.synchronize()
+            got = out.cpu().numpy()
+            assert np.isfinite(got).all()
+            assert G.norm_max_err(got, ref) <= TOL
+
+        # sizes beyond the static array are refused, not rendered
+        big = ctx.request(sid, tid, fg.METHOD_NN, 16, 16, 5000, 16, 0.1, 0.2, width)
+        rc = lib.fomo_render_noalloc(ctx.h, ctypes.byref(big), ctypes.c_void_p(out.data_ptr()), None)
+        assert rc == fg.EINVAL
+        assert "limits" in lib.fomo_last_error(ctx.h).decode()
