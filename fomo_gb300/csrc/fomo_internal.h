@@ -102,6 +102,10 @@ enum MarchStat {
   kStatSamples,        // LOS samples searched
   kStatScanned,        // candidates scanned by samples
   kStatTies,           // samples re-ranked in FP64
+  kStatFbNoCand,       // fallback reason: no in-box candidate within the coverage radius
+  kStatFbFar,          // fallback reason: best candidate beyond the coverage radius
+  kStatFbAmb,          // fallback reason: a candidate within a few ulp of a box face
+  kStatFbUnion,        // fallback samples resolved by the union-of-boxes gather
   kStatCount
 };
 

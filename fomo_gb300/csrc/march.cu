@@ -58,6 +58,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
+constexpr int kMinCtas = 4;  // resident CTAs per SM: 16 warps of latency hiding at <= 128 registers
 constexpr float kRelTie = 4e-6f;      // FP32 distance ambiguity band (>> FP32 + FP64 error)
 constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
@@ -66,11 +67,13 @@ constexpr int kSegCap = 256;          // candidates per segment
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule before the cooperative fallback
 constexpr float kRScale = 1.15f;      // gather radius in local point spacings
 
+constexpr int kUnionCap = 2 * kSegCap;  // points of the union-of-boxes list of a segment's fallback samples
+
 struct __align__(16) SegSmem {
-  float4 cq[kSegCap];  // gathered candidates
-  float4 sq[kSegCap];  // candidates sorted by the sample they project onto
-  int cpos[kSegCap];
-  int spos[kSegCap];
+  // [0, kSegCap): gathered candidates; [kSegCap, 2 kSegCap): the same sorted by
+  // the sample they project onto.  The union-of-boxes list uses all of it.
+  float4 q[kUnionCap];
+  int pos[kUnionCap];
   int bstart[kSeg + 1];
   int cursor[kSeg];
   unsigned char cb[kSegCap];
@@ -79,6 +82,20 @@ struct __align__(16) SegSmem {
 struct BoxQ {
   float tx, ty, tz, lox, loy, loz, hix, hiy, hiz;
 };
+
+__device__ __forceinline__ BoxQ shfl_box(const BoxQ& b, int src) {
+  BoxQ q;
+  q.tx = __shfl_sync(0xffffffffu, b.tx, src);
+  q.ty = __shfl_sync(0xffffffffu, b.ty, src);
+  q.tz = __shfl_sync(0xffffffffu, b.tz, src);
+  q.lox = __shfl_sync(0xffffffffu, b.lox, src);
+  q.loy = __shfl_sync(0xffffffffu, b.loy, src);
+  q.loz = __shfl_sync(0xffffffffu, b.loz, src);
+  q.hix = __shfl_sync(0xffffffffu, b.hix, src);
+  q.hiy = __shfl_sync(0xffffffffu, b.hiy, src);
+  q.hiz = __shfl_sync(0xffffffffu, b.hiz, src);
+  return q;
+}
 
 struct CellRange {
   int b0[3], b1[3], c[3];
@@ -261,9 +278,11 @@ __device__ __forceinline__ void coop_search(const SnapDev& S, const BoxQ& q, int
   coop_ring_pass<false>(S, q, R, gbest, 0.0f, lb1, lb2, lpos, lorig, lD, lDorig, lDpos);
   const float g1 = warp_min(lb1);
   if (!(g1 < FLT_MAX)) return;
+  const unsigned at_g1 = __ballot_sync(kFull, lb1 == g1);
   const float g2 = warp_min(lb1 == g1 ? lb2 : lb1);
-  if (g2 <= g1 * (1.0f + kRelTie)) {
-    // possible FP64 tie: exact re-rank of the contenders, lowest index wins
+  if (__popc(at_g1) > 1 || g2 <= g1 * (1.0f + kRelTie)) {
+    // possible FP64 tie (also two lanes at the same FP32 minimum): exact
+    // re-rank of the contenders, lowest index wins
     float fixed = g1;
     coop_ring_pass<true>(S, q, R, fixed, g1 * (1.0f + kRelTie), lb1, lb2, lpos, lorig, lD, lDorig, lDpos);
 #pragma unroll
@@ -280,10 +299,70 @@ __device__ __forceinline__ void coop_search(const SnapDev& S, const BoxQ& q, int
     *pos = lDpos;
     *orig = lDorig;
   } else {
-    const int w = __ffs(__ballot_sync(kFull, lb1 == g1)) - 1;
+    const int w = __ffs(at_g1) - 1;
     *pos = __shfl_sync(kFull, lpos, w);
     *orig = __shfl_sync(kFull, lorig, w);
   }
+}
+
+// Nearest point of the shared list lq[0, n) strictly inside the box q (the
+// same for all lanes), scanned by the whole warp; -1 when none.  Returns the
+// list slot to every lane.
+__device__ __forceinline__ int coop_list_search(const float4* lq, int n, const BoxQ& q) {
+  const int lane = threadIdx.x & 31;
+  float lb1 = FLT_MAX, lb2 = FLT_MAX;
+  int li = -1;
+  for (int c = lane; c < n; c += 32) {
+    const float4 v = lq[c];
+    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+      const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      if (d2 < lb1) {
+        lb2 = lb1;
+        lb1 = d2;
+        li = c;
+      } else if (d2 < lb2) {
+        lb2 = d2;
+      }
+    }
+  }
+  const float g1 = warp_min(lb1);
+  if (!(g1 < FLT_MAX)) return -1;
+  const unsigned at_g1 = __ballot_sync(kFull, lb1 == g1);
+  const float g2 = warp_min(lb1 == g1 ? lb2 : lb1);
+  if (__popc(at_g1) == 1 && g2 > g1 * (1.0f + kRelTie)) return __shfl_sync(kFull, li, __ffs(at_g1) - 1);
+  // possible FP64 tie: exact re-rank of the contenders, lowest original index wins
+  const float band = g1 * (1.0f + kRelTie);
+  double lD = DBL_MAX;
+  int lo = 0x7fffffff;
+  li = -1;
+  for (int c = lane; c < n; c += 32) {
+    const float4 v = lq[c];
+    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+      if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= band) {
+        const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
+        const int o = __float_as_int(v.w);
+        if (D < lD || (D == lD && o < lo)) {
+          lD = D;
+          lo = o;
+          li = c;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double D2 = __shfl_xor_sync(kFull, lD, o);
+    const int o2 = __shfl_xor_sync(kFull, lo, o);
+    const int c2 = __shfl_xor_sync(kFull, li, o);
+    if (D2 < lD || (D2 == lD && o2 < lo)) {
+      lD = D2;
+      lo = o2;
+      li = c2;
+    }
+  }
+  return li;
 }
 
 // ---------------------------------------------------------------------------
@@ -366,6 +445,32 @@ __device__ __forceinline__ BoxQ exact_box(const RayCtx& r, int k) {
   q.hiy = __double2float_rn(__dadd_rn(p1, r.md));
   q.hiz = __double2float_rn(__dadd_rn(p2, r.md));
   return q;
+}
+
+// Exact re-rank of a near-tie: among candidates [c0, c1) of the sorted list
+// that lie inside the box (Chebyshev distance below md_in) with FP32 distance
+// within `band`, the smallest FP64 distance, then the lowest original index.
+// Rare (a few samples per million), so kept out of line.
+__device__ __noinline__ int exact_rerank_list(const float4* sq, int c0, int c1, float tx, float ty, float tz,
+                                              float md_in, float band) {
+  double bestD = DBL_MAX;
+  int bestOrig = 0x7fffffff, bi = -1;
+  for (int c = c0; c < c1; ++c) {
+    const float4 q = sq[c];
+    const float dx = q.x - tx, dy = q.y - ty, dz = q.z - tz;
+    const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float cheb = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+    if (cheb < md_in && d2 <= band) {
+      const double D = exact_dist2(q.x, q.y, q.z, tx, ty, tz);
+      const int o = __float_as_int(q.w);
+      if (D < bestD || (D == bestD && o < bestOrig)) {
+        bestD = D;
+        bestOrig = o;
+        bi = c;
+      }
+    }
+  }
+  return bi;
 }
 
 // s-interval of the segment a + s d, s in [slo, shi], whose coordinate lies in [lo, hi].
@@ -503,8 +608,8 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
           if (keep) {
             const int slot = count + __popc(msk & lt);
             if (slot < kSegCap) {
-              sm.cq[slot] = q;
-              sm.cpos[slot] = p;
+              sm.q[slot] = q;
+              sm.pos[slot] = p;
               sm.cb[slot] = (unsigned char)bk;
             }
           }
@@ -534,11 +639,13 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
   }
   __syncwarp();
   for (int c = lane; c < ncand; c += 32) {
-    const int dst = atomicAdd(&sm.cursor[sm.cb[c]], 1);
-    sm.sq[dst] = sm.cq[c];
-    sm.spos[dst] = sm.cpos[c];
+    const int dst = kSegCap + atomicAdd(&sm.cursor[sm.cb[c]], 1);
+    sm.q[dst] = sm.q[c];
+    sm.pos[dst] = sm.pos[c];
   }
   __syncwarp();
+  const float4* sq = sm.q + kSegCap;  // the candidates in sample order
+  const int* spos = sm.pos + kSegCap;
   // ---- 3./4. per-sample scan of the buckets within R, acceptance
   const float dlt = (nseg > 1) ? len / (float)(nseg - 1) : 0.0f;
   const int w = (dlt > 0.0f) ? min((int)(Rg / dlt + 0.51f) + 1, kSeg) : kSeg;
@@ -563,7 +670,7 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
       int bi = -1;
       bool amb = false;
       for (int c = c0; c < c1; ++c) {
-        const float4 q = sm.sq[c];
+        const float4 q = sq[c];
         const float dx = q.x - t_x, dy = q.y - t_y, dz = q.z - t_z;
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float cheb = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
@@ -601,28 +708,13 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
         if (b2 <= b1 * (1.0f + kRelTie)) {
           // possible FP64 tie: exact re-rank of the in-box contenders
           ++st_ties;
-          const float band = b1 * (1.0f + kRelTie);
-          double bestD = DBL_MAX;
-          int bestOrig = 0x7fffffff;
-          for (int c = c0; c < c1; ++c) {
-            const float4 q = sm.sq[c];
-            const float dx = q.x - t_x, dy = q.y - t_y, dz = q.z - t_z;
-            const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const float cheb = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
-            if (cheb < md_in && d2 <= band) {
-              const double D = exact_dist2(q.x, q.y, q.z, t_x, t_y, t_z);
-              const int o = __float_as_int(q.w);
-              if (D < bestD || (D == bestD && o < bestOrig)) {
-                bestD = D;
-                bestOrig = o;
-                bi = c;
-              }
-            }
-          }
+          bi = exact_rerank_list(sq, c0, c1, t_x, t_y, t_z, md_in, b1 * (1.0f + kRelTie));
         }
-        pres = sm.spos[bi];
-        ores = __float_as_int(sm.sq[bi].w);
+        pres = spos[bi];
+        ores = __float_as_int(sq[bi].w);
       }
+      if (stats && !accept)  // rare: counted where it happens
+        atomicAdd(stats + (amb ? kStatFbAmb : (bi < 0 ? kStatFbNoCand : kStatFbFar)), 1ull);
     }
     st_samples += acti ? 1 : 0;
     const bool need = acti && !accept;
@@ -698,94 +790,48 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
           const unsigned msk = __ballot_sync(kFull, keep);
           if (keep) {
             const int slot = ucount + __popc(msk & lt);
-            if (slot < kSegCap) {
-              sm.sq[slot] = q;
-              sm.spos[slot] = p;
+            if (slot < kUnionCap) {
+              sm.q[slot] = q;
+              sm.pos[slot] = p;
             }
           }
           ucount += __popc(msk);
         }
       }
-      if (ucount > kSegCap) ok = false;
+      if (ucount > kUnionCap) ok = false;
     }
     __syncwarp();
-    if (ok) {
+    if (stats && ok && lane == 0) atomicAdd(stats + kStatFbUnion, (unsigned long long)(__popc(f0) + __popc(f1)));
+    // each remaining sample in turn, by the whole warp: a scan of the union
+    // list, or (6.) on overflow a ring search of the grid
 #pragma unroll 1
-      for (int i = 0; i < 2; ++i) {
-        if (i ? need1 : need0) {
-          const BoxQ q = exact_box(r, s0 + lane + 32 * i);
-          float b1 = FLT_MAX, b2 = FLT_MAX;
-          int bi = -1;
-          for (int c = 0; c < ucount; ++c) {
-            const float4 v = sm.sq[c];
-            if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-              const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-              const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-              if (d2 < b1) {
-                b2 = b1;
-                b1 = d2;
-                bi = c;
-              } else if (d2 < b2) {
-                b2 = d2;
-              }
-            }
-          }
-          if (bi >= 0 && b2 <= b1 * (1.0f + kRelTie)) {
-            // possible FP64 tie: exact re-rank, lowest original index wins
-            const float band = b1 * (1.0f + kRelTie);
-            double bestD = DBL_MAX;
-            int bestOrig = 0x7fffffff;
-            for (int c = 0; c < ucount; ++c) {
-              const float4 v = sm.sq[c];
-              if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-                const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-                if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= band) {
-                  const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
-                  const int o = __float_as_int(v.w);
-                  if (D < bestD || (D == bestD && o < bestOrig)) {
-                    bestD = D;
-                    bestOrig = o;
-                    bi = c;
-                  }
-                }
-              }
-            }
-          }
-          const int pres = bi >= 0 ? sm.spos[bi] : -1;
-          const int ores = bi >= 0 ? __float_as_int(sm.sq[bi].w) : -1;
-          if (i) {
-            pos[1] = pres;
-            orig[1] = ores;
-          } else {
-            pos[0] = pres;
-            orig[0] = ores;
-          }
-        }
-      }
-    }
-    __syncwarp();
-    if (!ok) {
-  // ---- 6. overflow: the remaining samples one at a time, by the whole warp
-#pragma unroll 1
-  for (int i = 0; i < 2; ++i) {
-    unsigned fm = i ? f1 : f0;
-    while (fm) {
-      const int sl = __ffs(fm) - 1;
-      fm &= fm - 1;
-      const BoxQ q = exact_box(r, s0 + sl + 32 * i);
-      int p, o;
-      coop_search(S, q, &p, &o);
-      if (lane == sl) {
-        if (i) {
-          pos[1] = p;
-          orig[1] = o;
+    for (int i = 0; i < 2; ++i) {
+      unsigned fm = i ? f1 : f0;
+      if (!fm) continue;
+      BoxQ mine = {};
+      if (i ? need1 : need0) mine = exact_box(r, s0 + lane + 32 * i);
+      while (fm) {
+        const int sl = __ffs(fm) - 1;
+        fm &= fm - 1;
+        const BoxQ q = shfl_box(mine, sl);
+        int p, o;
+        if (ok) {
+          const int c = coop_list_search(sm.q, ucount, q);
+          p = c >= 0 ? sm.pos[c] : -1;
+          o = c >= 0 ? __float_as_int(sm.q[c].w) : -1;
         } else {
-          pos[0] = p;
-          orig[0] = o;
+          coop_search(S, q, &p, &o);
+        }
+        if (lane == sl) {
+          if (i) {
+            pos[1] = p;
+            orig[1] = o;
+          } else {
+            pos[0] = p;
+            orig[0] = o;
+          }
         }
       }
-    }
-  }
     }
   }
   __syncwarp();  // the lists are rewritten by the next segment
@@ -818,7 +864,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 // `lane` owns bins wstart + 32 m + lane of each line.
 // ---------------------------------------------------------------------------
 template <int NL, int NB>
-__global__ void __launch_bounds__(kThreads) march_spectral(MarchArgs a, const double3* __restrict__ ktab,
+__global__ void __launch_bounds__(kThreads, kMinCtas) march_spectral(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride) {
   __shared__ SegSmem segs[kWarps];
   SegSmem& sm = segs[threadIdx.x >> 5];
@@ -948,7 +994,7 @@ __global__ void __launch_bounds__(kThreads) march_spectral(MarchArgs a, const do
 // reduced across the warp per 32-sample chunk, Kahan-accumulated per ray.
 // ---------------------------------------------------------------------------
 template <int NL, bool THOMSON>
-__global__ void __launch_bounds__(kThreads) march_imaging(MarchArgs a, const double3* __restrict__ ktab,
+__global__ void __launch_bounds__(kThreads, kMinCtas) march_imaging(MarchArgs a, const double3* __restrict__ ktab,
                                                           int ktab_stride) {
   __shared__ SegSmem segs[kWarps];
   SegSmem& sm = segs[threadIdx.x >> 5];

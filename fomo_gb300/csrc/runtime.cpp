@@ -912,9 +912,11 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
     cudaMemcpy(h, ctx->march_stats, sizeof(h), cudaMemcpyDeviceToHost);
     std::fprintf(stderr,
                  "fomo march stats: segments %llu candidates %llu rows %llu points_loaded %llu not_gathered %llu "
-                 "fallbacks %llu samples %llu scanned %llu ties %llu\n",
+                 "fallbacks %llu (ambiguous %llu no_candidate %llu far %llu union %llu) samples %llu scanned %llu "
+                 "ties %llu\n",
                  h[kStatSegments], h[kStatCandidates], h[kStatRows], h[kStatPointsLoaded], h[kStatNotGathered],
-                 h[kStatFallbacks], h[kStatSamples], h[kStatScanned], h[kStatTies]);
+                 h[kStatFallbacks], h[kStatFbAmb], h[kStatFbNoCand], h[kStatFbFar], h[kStatFbUnion],
+                 h[kStatSamples], h[kStatScanned], h[kStatTies]);
     cudaFree(ctx->march_stats);
   }
   ctx->scratch.release();
