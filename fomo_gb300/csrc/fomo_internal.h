@@ -75,6 +75,15 @@ struct LineDesc {
   int nw;                    // 32-bin windows evaluated; other bins are below 2^-64 of every peak
 };
 
+// Work counters of one march (zeroed before it): the ray queue head, the number
+// of deferred-sample records written, the deferred-record queue head.
+enum MarchCounter { kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrCount };
+
+// One segment whose samples the march's first search pass could not resolve:
+// x = work item of the ray, y = first LOS sample of the segment, z/w = masks
+// of the unresolved samples y + lane and y + 32 + lane.
+using DeferredRec = uint4;
+
 struct MarchArgs {
   SnapDev snap;
   ViewDesc* views;           // nviews
@@ -82,8 +91,11 @@ struct MarchArgs {
   const LineDesc* lines;     // nviews * nlines
   int nviews;
   int nlines;
-  int64_t total_items;
-  unsigned long long* counter;   // work-queue head, zeroed before the launch
+  int64_t item_base;         // first work item of this launch (item ranges of one plan)
+  int64_t total_items;       // one past the last work item
+  unsigned long long* counter;   // kCtrCount work counters, zeroed before the launch
+  DeferredRec* deferred;         // one record per segment at most: capacity deferred_cap
+  int64_t deferred_cap;
   int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
@@ -106,6 +118,7 @@ enum MarchStat {
   kStatFbFar,          // fallback reason: best candidate beyond the coverage radius
   kStatFbAmb,          // fallback reason: a candidate within a few ulp of a box face
   kStatFbUnion,        // fallback samples resolved by the union-of-boxes gather
+  kStatDeferredRecs,   // deferred-sample records (segments with fallback samples)
   kStatCount
 };
 
@@ -151,8 +164,13 @@ cudaError_t launch_view_extents(SnapDev snap, ViewDesc* views, int nviews, float
 cudaError_t launch_view_finalize(ViewDesc* views, int nviews, double3* ktab, int ktab_stride, cudaStream_t s);
 
 // march.cu
+// The march: the first search pass and the emission sums of every ray, then
+// the deferred samples' nearest neighbours and their contributions (a second
+// kernel on the same stream).
 cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
                          cudaStream_t s, int blocks_per_sm_hint, bool imaging);
 int march_bins_per_lane(int nlines, int L);
+// Capacity of the deferred-record queue for `items` work items of up to nz samples.
+inline int64_t deferred_capacity(int64_t items, int nz) { return items * ((nz + 63) / 64); }
 
 }  // namespace fomo

@@ -371,6 +371,7 @@ __device__ __forceinline__ int coop_list_search(const float4* lq, int n, const B
 
 struct RayCtx {
   int v, i, j;
+  unsigned int item;  // work item of the ray (recorded with its deferred samples)
   double A0, A1, A2, md;
   float mdf;
   const double3* kt;
@@ -387,38 +388,48 @@ __device__ __forceinline__ int find_view(const int64_t* off, int nviews, int64_t
 }
 
 // Next ray for this warp; false when the queue is drained.
+// The ray of work item `item` (views' rays in tile order); false for the
+// padding items of partial tiles.
+__device__ __forceinline__ bool ray_of_item(const MarchArgs& a, const double3* ktab, int ktab_stride,
+                                            int64_t item, RayCtx& r) {
+  const int v = find_view(a.ray_offset, a.nviews, item);
+  const ViewDesc* V = a.views + v;
+  const int nx = V->nx, ny = V->ny, tw = V->ray_tile_w, th = V->ray_tile_h;
+  const int local = (int)(item - __ldg(a.ray_offset + v));  // < nx*ny < 2^31
+  const int tiles_x = (nx + tw - 1) / tw;
+  const int tile = local / (tw * th);
+  const int within = local - tile * (tw * th);
+  const int i = (tile / tiles_x) * th + within / tw;
+  const int j = (tile % tiles_x) * tw + within % tw;
+  if (i >= ny || j >= nx) return false;
+  // ray position in the image plane (nn:152-153, tabulated per view by the
+  // finalize kernel) and the per-ray terms of the derotation (nn:165)
+  const double x = V->xt[j];
+  const double y = V->yt[i];
+  const double cb = V->cb, sb = V->sb, cl = V->cl, sl = V->sl;
+  r.v = v;
+  r.i = i;
+  r.j = j;
+  r.item = (unsigned int)item;
+  r.A0 = __dadd_rn(__dmul_rn(__dmul_rn(x, cb), cl), __dmul_rn(y, sl));
+  r.A1 = __dadd_rn(__dmul_rn(__dmul_rn(-x, cb), sl), __dmul_rn(y, cl));
+  r.A2 = __dmul_rn(-x, sb);
+  r.md = V->md;
+  r.mdf = __double2float_rn(V->md);
+  r.kt = ktab + (int64_t)v * ktab_stride;
+  return true;
+}
+
+// Warp-collective: the next ray of the work queue (items item_base ..
+// total_items - 1), false when the queue is drained.
 __device__ __forceinline__ bool next_ray(const MarchArgs& a, const double3* ktab, int ktab_stride, RayCtx& r) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long item = 0;
-    if (lane == 0) item = atomicAdd(a.counter, 1ull);
-    item = __shfl_sync(kFull, item, 0);
+    if (lane == 0) item = atomicAdd(a.counter + kCtrRays, 1ull);
+    item = __shfl_sync(kFull, item, 0) + (unsigned long long)a.item_base;
     if ((int64_t)item >= a.total_items) return false;
-    const int v = find_view(a.ray_offset, a.nviews, (int64_t)item);
-    const ViewDesc* V = a.views + v;
-    const int nx = V->nx, ny = V->ny, tw = V->ray_tile_w, th = V->ray_tile_h;
-    const int local = (int)((int64_t)item - __ldg(a.ray_offset + v));  // < nx*ny < 2^31
-    const int tiles_x = (nx + tw - 1) / tw;
-    const int tile = local / (tw * th);
-    const int within = local - tile * (tw * th);
-    const int i = (tile / tiles_x) * th + within / tw;
-    const int j = (tile % tiles_x) * tw + within % tw;
-    if (i >= ny || j >= nx) continue;
-    // ray position in the image plane (nn:152-153, tabulated per view by the
-    // finalize kernel) and the per-ray terms of the derotation (nn:165)
-    const double x = V->xt[j];
-    const double y = V->yt[i];
-    const double cb = V->cb, sb = V->sb, cl = V->cl, sl = V->sl;
-    r.v = v;
-    r.i = i;
-    r.j = j;
-    r.A0 = __dadd_rn(__dmul_rn(__dmul_rn(x, cb), cl), __dmul_rn(y, sl));
-    r.A1 = __dadd_rn(__dmul_rn(__dmul_rn(-x, cb), sl), __dmul_rn(y, cl));
-    r.A2 = __dmul_rn(-x, sb);
-    r.md = V->md;
-    r.mdf = __double2float_rn(V->md);
-    r.kt = ktab + (int64_t)v * ktab_stride;
-    return true;
+    if (ray_of_item(a, ktab, ktab_stride, (int64_t)item, r)) return true;
   }
 }
 
@@ -488,8 +499,12 @@ __device__ __forceinline__ void clip_interval(float a, float d, float inv_d, flo
 
 // Warp-collective: nearest neighbours of the segment's samples s0 .. s0+63.
 // pos[i]/orig[i] are this lane's results for sample s0 + lane + 32 i.
-__device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r, int s0, int nz, SegSmem& sm,
-                                               int (&pos)[2], int (&orig)[2], unsigned long long* stats) {
+// Samples it cannot resolve get no neighbour here (-1) and are recorded in
+// the deferred queue.
+__device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx& r, int s0, int nz, SegSmem& sm,
+                                               int (&pos)[2], int (&orig)[2]) {
+  const SnapDev& S = a.snap;
+  unsigned long long* const stats = a.stats;
   int st_rows = 0, st_loaded = 0, st_scanned = 0, st_ties = 0, st_samples = 0;
   const int lane = threadIdx.x & 31;
   const GridParams& g = S.g;
@@ -728,24 +743,59 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
       need0 = need;
     }
   }
-  __syncwarp();  // the candidate lists are reused below and by the next segment
-  // ---- 5. the remaining samples: gather the points of the union of their
-  // boxes once, then every such sample scans that list with its exact box
+  __syncwarp();  // the candidate lists are rewritten by the next segment
+  // ---- 5. samples this pass could not resolve (about 1 %) are left empty
+  // here and deferred to the second kernel: one record per segment
   const unsigned f0 = __ballot_sync(kFull, need0), f1 = __ballot_sync(kFull, need1);
-  if (f0 | f1) {
+  if ((f0 | f1) && lane == 0) {
+    const unsigned long long slot = atomicAdd(a.counter + kCtrDeferred, 1ull);
+    if ((int64_t)slot < a.deferred_cap)  // always: the capacity is one record per segment
+      a.deferred[slot] = make_uint4(r.item, (unsigned)s0, f0, f1);
+  }
+  if (stats) {
+    const unsigned sc = __reduce_add_sync(kFull, (unsigned)st_scanned);
+    const unsigned ti = __reduce_add_sync(kFull, (unsigned)st_ties);
+    const unsigned sa = __reduce_add_sync(kFull, (unsigned)st_samples);
+    if (lane == 0) {
+      atomicAdd(stats + kStatSegments, 1ull);
+      atomicAdd(stats + kStatCandidates, (unsigned long long)count);
+      atomicAdd(stats + kStatRows, (unsigned long long)st_rows);
+      atomicAdd(stats + kStatPointsLoaded, (unsigned long long)st_loaded);
+      atomicAdd(stats + kStatNotGathered, gathered ? 0ull : 1ull);
+      atomicAdd(stats + kStatFallbacks, (unsigned long long)(__popc(f0) + __popc(f1)));
+      atomicAdd(stats + kStatDeferredRecs, (f0 | f1) ? 1ull : 0ull);
+      atomicAdd(stats + kStatSamples, (unsigned long long)sa);
+      atomicAdd(stats + kStatScanned, (unsigned long long)sc);
+      atomicAdd(stats + kStatTies, (unsigned long long)ti);
+    }
+  }
+}
+
+// Warp-collective: nearest neighbours of the deferred samples s0 + lane
+// (mask f0) and s0 + 32 + lane (mask f1) of ray r.  The points of the union
+// of their exact boxes are gathered once, then every such sample in turn is
+// searched in that list by the whole warp; when the union holds too many
+// points, each sample is searched by a ring search of the grid instead.
+__device__ __forceinline__ void resolve_deferred(const SnapDev& S, const RayCtx& r, int s0, unsigned f0, unsigned f1,
+                                                 SegSmem& sm, int (&pos)[2], int (&orig)[2],
+                                                 unsigned long long* stats) {
+  const int lane = threadIdx.x & 31;
+  const GridParams& g = S.g;
+  const bool need0 = (f0 >> lane) & 1u, need1 = (f1 >> lane) & 1u;
+  {
+    BoxQ mb[2];
     float ulx = FLT_MAX, uly = FLT_MAX, ulz = FLT_MAX, uhx = -FLT_MAX, uhy = -FLT_MAX, uhz = -FLT_MAX;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
+      mb[i] = BoxQ{};
       if (i ? need1 : need0) {
-        const float t_x = i ? tx[1] : tx[0], t_y = i ? ty[1] : ty[0], t_z = i ? tz[1] : tz[0];
-        const float tmax = fmaxf(fmaxf(fabsf(t_x), fabsf(t_y)), fabsf(t_z));
-        const float mo = r.mdf + (tmax + r.mdf) * 4.8e-7f + r.mdf * 1.2e-7f;  // superset of the exact box
-        ulx = fminf(ulx, t_x - mo);
-        uly = fminf(uly, t_y - mo);
-        ulz = fminf(ulz, t_z - mo);
-        uhx = fmaxf(uhx, t_x + mo);
-        uhy = fmaxf(uhy, t_y + mo);
-        uhz = fmaxf(uhz, t_z + mo);
+        mb[i] = exact_box(r, s0 + lane + 32 * i);
+        ulx = fminf(ulx, mb[i].lox);
+        uly = fminf(uly, mb[i].loy);
+        ulz = fminf(ulz, mb[i].loz);
+        uhx = fmaxf(uhx, mb[i].hix);
+        uhy = fmaxf(uhy, mb[i].hiy);
+        uhz = fmaxf(uhz, mb[i].hiz);
       }
     }
     ulx = fmaxf(warp_min(ulx), g.minx);
@@ -802,18 +852,15 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
     }
     __syncwarp();
     if (stats && ok && lane == 0) atomicAdd(stats + kStatFbUnion, (unsigned long long)(__popc(f0) + __popc(f1)));
-    // each remaining sample in turn, by the whole warp: a scan of the union
-    // list, or (6.) on overflow a ring search of the grid
+    // each deferred sample in turn, by the whole warp: a scan of the union
+    // list, or on overflow a ring search of the grid
 #pragma unroll 1
     for (int i = 0; i < 2; ++i) {
       unsigned fm = i ? f1 : f0;
-      if (!fm) continue;
-      BoxQ mine = {};
-      if (i ? need1 : need0) mine = exact_box(r, s0 + lane + 32 * i);
       while (fm) {
         const int sl = __ffs(fm) - 1;
         fm &= fm - 1;
-        const BoxQ q = shfl_box(mine, sl);
+        const BoxQ q = shfl_box(i ? mb[1] : mb[0], sl);
         int p, o;
         if (ok) {
           const int c = coop_list_search(sm.q, ucount, q);
@@ -834,23 +881,7 @@ __device__ __forceinline__ void segment_search(const SnapDev& S, const RayCtx& r
       }
     }
   }
-  __syncwarp();  // the lists are rewritten by the next segment
-  if (stats) {
-    const unsigned sc = __reduce_add_sync(kFull, (unsigned)st_scanned);
-    const unsigned ti = __reduce_add_sync(kFull, (unsigned)st_ties);
-    const unsigned sa = __reduce_add_sync(kFull, (unsigned)st_samples);
-    if (lane == 0) {
-      atomicAdd(stats + kStatSegments, 1ull);
-      atomicAdd(stats + kStatCandidates, (unsigned long long)count);
-      atomicAdd(stats + kStatRows, (unsigned long long)st_rows);
-      atomicAdd(stats + kStatPointsLoaded, (unsigned long long)st_loaded);
-      atomicAdd(stats + kStatNotGathered, gathered ? 0ull : 1ull);
-      atomicAdd(stats + kStatFallbacks, (unsigned long long)(__popc(f0) + __popc(f1)));
-      atomicAdd(stats + kStatSamples, (unsigned long long)sa);
-      atomicAdd(stats + kStatScanned, (unsigned long long)sc);
-      atomicAdd(stats + kStatTies, (unsigned long long)ti);
-    }
-  }
+  __syncwarp();  // the list is rewritten by the next record
 }
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -901,7 +932,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_spectral(MarchArgs a
     const int64_t ray = (int64_t)r.i * nx + r.j;
     for (int s0 = 0; s0 < nz; s0 += kSeg) {
       int posv[2], origv[2];
-      segment_search(a.snap, r, s0, nz, sm, posv, origv, a.stats);
+      segment_search(a, r, s0, nz, sm, posv, origv);
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
         const int k = s0 + 32 * h + lane;
@@ -1017,7 +1048,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_imaging(MarchArgs a,
     const int64_t ray = (int64_t)r.i * nx + r.j;
     for (int s0 = 0; s0 < nz; s0 += kSeg) {
       int posv[2], origv[2];
-      segment_search(a.snap, r, s0, nz, sm, posv, origv, a.stats);
+      segment_search(a, r, s0, nz, sm, posv, origv);
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
         const int k = s0 + 32 * h + lane;
@@ -1051,6 +1082,110 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_imaging(MarchArgs a,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Deferred samples: the march's first pass leaves about 1 % of the samples
+// (boxes reaching past its gather radius, mostly just outside the point
+// cloud) empty and records them.  This kernel finds their neighbours, writes
+// their NN indices and adds their emission to the rays' outputs, which the
+// march has already written (same stream, so after it).  One warp per record.
+// ---------------------------------------------------------------------------
+enum DeferredKind : int { kDeferredSpectral = 0, kDeferredImaging = 1, kDeferredThomson = 2 };
+
+__global__ void __launch_bounds__(kThreads) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
+                                                           int ktab_stride, int kind) {
+  __shared__ SegSmem segs[kWarps];
+  __shared__ int fpos[kWarps][kSeg];    // the record's deferred samples: neighbour (sorted position)
+  __shared__ float fvlos[kWarps][kSeg]; // and its LOS speed
+  const int w = threadIdx.x >> 5;
+  SegSmem& sm = segs[w];
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t nrec = min((int64_t)a.counter[kCtrDeferred], a.deferred_cap);  // written by the march
+  for (;;) {
+    unsigned long long idx = 0;
+    if (lane == 0) idx = atomicAdd(a.counter + kCtrDeferredHead, 1ull);
+    idx = __shfl_sync(kFull, idx, 0);
+    if ((int64_t)idx >= nrec) return;
+    const DeferredRec rec = a.deferred[idx];
+    RayCtx r;
+    if (!ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, r)) continue;  // records come from real rays only
+    const int s0 = (int)rec.y;
+    const unsigned f0 = rec.z, f1 = rec.w;
+    int pos[2] = {-1, -1}, orig[2] = {-1, -1};
+    resolve_deferred(a.snap, r, s0, f0, f1, sm, pos, orig, a.stats);
+    const ViewDesc* V = a.views + r.v;
+    const int nz = V->nz, nx = V->nx;
+    const int64_t ray = (int64_t)r.i * nx + r.j;
+    const bool need0 = (f0 >> lane) & 1u, need1 = (f1 >> lane) & 1u;
+    int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+    if (nnout) {
+      if (need0) nnout[ray * nz + s0 + lane] = orig[0];
+      if (need1) nnout[ray * nz + s0 + 32 + lane] = orig[1];
+    }
+    const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
+    if (kind == kDeferredSpectral) {
+      // the deferred samples as a compact list, then lane = lambda bin as in
+      // the march (each sample is its own run)
+      const int n0 = __popc(f0), nf = n0 + __popc(f1);
+      const float ux = V->ux, uy = V->uy, uz = V->uz;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        if (i ? need1 : need0) {
+          const int slot = i ? n0 + __popc(f1 & lt) : __popc(f0 & lt);
+          const int p = i ? pos[1] : pos[0];
+          float vl = 0.0f;
+          if (p >= 0) {
+            const float4 vv = __ldg(a.snap.vel + p);
+            vl = fmaf(uz, vv.z, fmaf(uy, vv.y, ux * vv.x));
+          }
+          fpos[w][slot] = p;
+          fvlos[w][slot] = vl;
+        }
+      }
+      __syncwarp();
+      const int L = V->L;
+      for (int l = 0; l < a.nlines; ++l) {
+        const LineDesc& D = LD[l];
+        if (!D.ew) continue;  // views may have fewer lines than the launch
+        const double scale = D.is_dn ? V->scale_dn : V->scale;
+        for (int m = 0; m < D.nw; ++m) {
+          const int il = D.wstart + 32 * m + lane;
+          const float lamv = il < L ? __ldg(D.lam + il) : 3.0e30f;
+          float part = 0.0f;
+          for (int f = 0; f < nf; ++f) {
+            const int p = fpos[w][f];
+            if (p < 0) continue;
+            const float2 pw = __ldg(D.ew + p);
+            if (pw.x == 0.0f) continue;  // intpolpeak ? ... : 0 (nn:204)
+            const float sc = __fdividef(2.0f, pw.y);
+            const float ns = -(fvlos[w][f] * D.shift_k) * sc;
+            const float q = fmaf(lamv, sc, ns);
+            part = fmaf(pw.x, ex2_approx(-q * q), part);
+          }
+          if (il < L && part != 0.0f) atomicAdd(D.out + ray * L + il, __double2float_rn(__dmul_rn(scale, (double)part)));
+        }
+      }
+      __syncwarp();  // fpos/fvlos are rewritten by the next record
+    } else {
+      const float* s2v = kind == kDeferredThomson ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
+      for (int l = 0; l < a.nlines; ++l) {
+        const LineDesc& D = LD[l];
+        if (!D.out) continue;
+        float val = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const int p = i ? pos[1] : pos[0];
+          if ((i ? need1 : need0) && p >= 0)
+            val += s2v ? fmaxf(__ldg(a.totpol + p).y * __ldg(s2v + p), 0.0f) : __ldg(D.ew + p).x;
+        }
+        const float sum = warp_sum(val);
+        if (lane == 0 && sum != 0.0f)
+          atomicAdd(D.out + ray, __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
+      }
+    }
+  }
+}
+
 template <typename K>
 cudaError_t launch_persistent(K kernel, const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count,
                               cudaStream_t s, int blocks_per_sm_hint) {
@@ -1060,23 +1195,27 @@ cudaError_t launch_persistent(K kernel, const MarchArgs& a, const double3* ktab,
   if (per_sm < 1) per_sm = 1;
   if (blocks_per_sm_hint > 0 && blocks_per_sm_hint < per_sm) per_sm = blocks_per_sm_hint;
   int64_t blocks = (int64_t)sm_count * per_sm;
-  const int64_t cap = (a.total_items + kWarps - 1) / kWarps;
+  const int64_t cap = (a.total_items - a.item_base + kWarps - 1) / kWarps;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   kernel<<<(unsigned)blocks, kThreads, 0, s>>>(a, ktab, ktab_stride);
   return cudaGetLastError();
 }
 
-}  // namespace
-
-int march_bins_per_lane(int nlines, int L) {
-  (void)nlines;
-  return (L + 31) / 32;
+cudaError_t launch_deferred(const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count, cudaStream_t s,
+                            int kind) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_deferred, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  // the record count is known on the device only: a persistent grid that
+  // drains the queue (and exits at once when it is empty)
+  march_deferred<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
+  return cudaGetLastError();
 }
 
-// max_windows: largest number of 32-bin lambda windows of any line (1 for imaging).
-cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
-                         cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
+cudaError_t launch_first_pass(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows,
+                              int sm_count, cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
   const bool thomson = a.s2 != nullptr;
   if (thomson) return launch_persistent(march_imaging<1, true>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
   if (imaging) {
@@ -1101,6 +1240,23 @@ cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_strid
   FOMO_SPEC(4, 4);
 #undef FOMO_SPEC
   return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+int march_bins_per_lane(int nlines, int L) {
+  (void)nlines;
+  return (L + 31) / 32;
+}
+
+// max_windows: largest number of 32-bin lambda windows of any line (1 for imaging).
+cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
+                         cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
+  if (!a.deferred || a.deferred_cap <= 0 || !a.counter) return cudaErrorInvalidValue;
+  cudaError_t e = launch_first_pass(a, ktab, ktab_stride, max_windows, sm_count, s, blocks_per_sm_hint, imaging);
+  if (e != cudaSuccess) return e;
+  const int kind = a.s2 ? kDeferredThomson : (imaging ? kDeferredImaging : kDeferredSpectral);
+  return launch_deferred(a, ktab, ktab_stride, sm_count, s, kind);
 }
 
 }  // namespace fomo

@@ -9,7 +9,8 @@
 // grows with cudaMalloc when a larger render comes along.  This entry point
 // instead places that working memory -- the view and line descriptors, the
 // lambda table, the per-sample derotation table, the per-ray position tables
-// and the work counter -- in one file-scope static __device__ array of fixed
+// the work counters and the deferred-sample queue (whose fixed capacity makes
+// a large render march its rays in chunks) -- in one file-scope static __device__ array of fixed
 // size, so a call never allocates.
 //
 // The array costs every GPU that loads the library kNoAllocScratchBytes of
@@ -17,7 +18,7 @@
 // with cudaGetSymbolAddress once per device, on the first call made on that
 // device (that first call should therefore come before any stream capture).
 // Every call on a device shares the same array and the array keeps the last
-// call's contents: the work counter is cleared by each call, the per-view
+// call's contents: the work counters are cleared by each chunk, the per-view
 // extents are initialised by a kernel of each call, everything else is fully
 // rewritten.  Calls that overlap on the GPU (e.g. on two streams) race on the
 // array; serialise them.
@@ -26,6 +27,7 @@
 // march); only the place of their scratch differs.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -48,11 +50,15 @@ constexpr size_t kOffRayOff = align_up(kOffLine + sizeof(LineDesc));
 constexpr size_t kOffLam = align_up(kOffRayOff + 2 * sizeof(int64_t));
 constexpr size_t kHdrBytes = align_up(kOffLam + kNoAllocMaxL * sizeof(float));  // uploaded per call
 constexpr size_t kOffCounter = kHdrBytes;
-constexpr size_t kOffKtab = align_up(kOffCounter + 2 * sizeof(unsigned long long));
+constexpr size_t kOffKtab = align_up(kOffCounter + kCtrCount * sizeof(unsigned long long));
 constexpr size_t kOffXY = align_up(kOffKtab + (size_t)kNoAllocMaxNz * sizeof(double3));
-constexpr size_t kNoAllocScratchBytes = align_up(kOffXY + (size_t)kNoAllocMaxNxNy * sizeof(double));
+constexpr size_t kOffDeferred = align_up(kOffXY + (size_t)kNoAllocMaxNxNy * sizeof(double));
+// Deferred-sample queue: the rays are marched in chunks of at most
+// kNoAllocDeferredCap segments (1024 rays at the largest nz).
+constexpr int64_t kNoAllocDeferredCap = 65536;
+constexpr size_t kNoAllocScratchBytes = align_up(kOffDeferred + (size_t)kNoAllocDeferredCap * sizeof(DeferredRec));
 
-// The scratch of fomo_render_noalloc (about 167 KB per device).
+// The scratch of fomo_render_noalloc (about 1.2 MB per device).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;
@@ -134,7 +140,6 @@ extern "C" int fomo_render_noalloc(fomo_ctx* ctx, const fomo_request* req, float
   double3* ktab = reinterpret_cast<double3*>(base + kOffKtab);
   unsigned long long* counter = reinterpret_cast<unsigned long long*>(base + kOffCounter);
   e = cudaMemcpyAsync(base, hdr, kHdrBytes, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), s);
   const SnapDev sd = snap_dev(snap);
   if (e == cudaSuccess) e = launch_view_init(dv, 1, s);
   if (e == cudaSuccess) e = launch_view_extents(sd, dv, 1, nullptr, s);
@@ -147,9 +152,16 @@ extern "C" int fomo_render_noalloc(fomo_ctx* ctx, const fomo_request* req, float
   a.lines = reinterpret_cast<const LineDesc*>(base + kOffLine);
   a.nviews = 1;
   a.nlines = 1;
-  a.total_items = hoff[1];
   a.counter = counter;
-  if (e == cudaSuccess) e = launch_march(a, ktab, q.nz, hl->nw, ctx->sm_count, s, 0, imaging != 0);
+  a.deferred = reinterpret_cast<DeferredRec*>(base + kOffDeferred);
+  a.deferred_cap = kNoAllocDeferredCap;
+  const int64_t chunk = kNoAllocDeferredCap / ((q.nz + 63) / 64);  // rays whose segments fit the queue
+  for (int64_t b = 0; b < hoff[1] && e == cudaSuccess; b += chunk) {
+    a.item_base = b;
+    a.total_items = std::min<int64_t>(b + chunk, hoff[1]);
+    e = cudaMemsetAsync(counter, 0, kCtrCount * sizeof(unsigned long long), s);
+    if (e == cudaSuccess) e = launch_march(a, ktab, q.nz, hl->nw, ctx->sm_count, s, 0, imaging != 0);
+  }
   if (e != cudaSuccess) return cuda_err(ctx, e, "fomo_render_noalloc launch");
   return FOMO_OK;
 }

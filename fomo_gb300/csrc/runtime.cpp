@@ -676,7 +676,14 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     SnapRec& snap = ctx->snaps[G.snapshot];
     G.o_ktab = L.take(sizeof(double3) * (size_t)G.nv * G.maxnz);
     G.o_xy = L.take(sizeof(double) * (size_t)G.nv * (G.maxnx + G.maxny));
-    G.o_ctr = L.take(sizeof(unsigned long long) * 2);
+    G.o_ctr = L.take(sizeof(unsigned long long) * kCtrCount);
+    int64_t items = 0;
+    for (auto& v : G.vreqs) {
+      const fomo_request& q = reqs[v[0]];
+      items += (int64_t)((q.nx + G.tw - 1) / G.tw) * G.tw * (int64_t)((q.ny + G.th - 1) / G.th) * G.th;
+    }
+    G.deferred_cap = deferred_capacity(items, G.maxnz);
+    G.o_def = L.take(sizeof(DeferredRec) * (size_t)G.deferred_cap);
     G.o_s2 = G.method == FOMO_METHOD_THOMSON ? L.take(sizeof(float) * (size_t)G.nv * snap.n) : 0;
   }
   plan->dev_bytes = L.off;
@@ -770,7 +777,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s)
   for (const PlanGroup& G : plan.groups) {
     if (e != cudaSuccess) break;
     SnapRec& snap = ctx->snaps[G.snapshot];
-    e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * 2, s);
+    e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * kCtrCount, s);
     ViewDesc* dv = reinterpret_cast<ViewDesc*>(db + G.o_views);
     if (e == cudaSuccess) e = launch_view_init(dv, G.nv, s);
     SnapDev sd = snap_dev(snap);
@@ -786,8 +793,11 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s)
     a.lines = reinterpret_cast<const LineDesc*>(db + G.o_lines);
     a.nviews = G.nv;
     a.nlines = G.nl;
+    a.item_base = 0;
     a.total_items = G.total_items;
     a.counter = reinterpret_cast<unsigned long long*>(db + G.o_ctr);
+    a.deferred = reinterpret_cast<DeferredRec*>(db + G.o_def);
+    a.deferred_cap = G.deferred_cap;
     a.nn_idx = G.any_nn ? reinterpret_cast<int32_t* const*>(db + G.o_nnp) : nullptr;
     a.s2 = s2;
     a.totpol = G.totpol;
@@ -912,11 +922,11 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
     cudaMemcpy(h, ctx->march_stats, sizeof(h), cudaMemcpyDeviceToHost);
     std::fprintf(stderr,
                  "fomo march stats: segments %llu candidates %llu rows %llu points_loaded %llu not_gathered %llu "
-                 "fallbacks %llu (ambiguous %llu no_candidate %llu far %llu union %llu) samples %llu scanned %llu "
-                 "ties %llu\n",
+                 "fallbacks %llu (ambiguous %llu no_candidate %llu far %llu union %llu records %llu) samples %llu "
+                 "scanned %llu ties %llu\n",
                  h[kStatSegments], h[kStatCandidates], h[kStatRows], h[kStatPointsLoaded], h[kStatNotGathered],
                  h[kStatFallbacks], h[kStatFbAmb], h[kStatFbNoCand], h[kStatFbFar], h[kStatFbUnion],
-                 h[kStatSamples], h[kStatScanned], h[kStatTies]);
+                 h[kStatDeferredRecs], h[kStatSamples], h[kStatScanned], h[kStatTies]);
     cudaFree(ctx->march_stats);
   }
   ctx->scratch.release();

@@ -89,8 +89,10 @@ struct fomo_server {
 namespace {
 
 size_t request_cost(const fomo_request& q) {
-  // output cube + per-view descriptors and tables (generous)
-  return cube_elems(q) * sizeof(float) + (size_t)q.nz * 24 + (size_t)(q.nx + q.ny) * 8 + 64 * 1024;
+  // output cube + per-view descriptors and tables (generous) + the deferred-sample queue
+  const size_t rays = (size_t)(q.nx + 31) * (size_t)(q.ny + 31);  // tile padding included
+  return cube_elems(q) * sizeof(float) + (size_t)q.nz * 24 + (size_t)(q.nx + q.ny) * 8 + 64 * 1024 +
+         rays * (size_t)((q.nz + 63) / 64) * sizeof(DeferredRec);
 }
 
 void finish_slot(fomo_server* S, Slot& sl, int status) {
