@@ -65,7 +65,7 @@ constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning e
 constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
 constexpr int kSegCap = 256;          // candidates per segment
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule before the cooperative fallback
-constexpr float kRScale = 1.15f;      // gather radius in local point spacings
+constexpr float kRScale = 1.0f;       // gather radius in local point spacings
 
 constexpr int kUnionCap = 2 * kSegCap;  // points of the union-of-boxes list of a segment's fallback samples
 
@@ -898,7 +898,9 @@ template <int NL, int NB>
 __global__ void __launch_bounds__(kThreads, kMinCtas) march_spectral(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride) {
   __shared__ SegSmem segs[kWarps];
-  SegSmem& sm = segs[threadIdx.x >> 5];
+  __shared__ float4 runs[kWarps][32][NL];  // a chunk's runs: (peak x length, 2/w, Doppler term) per line
+  const int w = threadIdx.x >> 5;
+  SegSmem& sm = segs[w];
   const int lane = threadIdx.x & 31;
   RayCtx r;
   while (next_ray(a, ktab, ktab_stride, r)) {
@@ -946,53 +948,49 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_spectral(MarchArgs a
         const unsigned act = __ballot_sync(kFull, active);
         if (!act) break;
         const int endlane = 32 - __clz(act);
-        // the start lane of each run loads its payload and forms the per-line terms
-        float rpk[NL], rsc[NL], rns[NL];
-#pragma unroll
-        for (int l = 0; l < NL; ++l) {
-          rpk[l] = 0.0f;
-          rsc[l] = 0.0f;
-          rns[l] = 0.0f;
-        }
-        if (start && pos >= 0) {
+        // the start lane of each run with a neighbour loads its payload and
+        // stages the per-line terms (peak x run length, 2/w, Doppler offset)
+        // in a compact list; a peak of 0 (intpolpeak ? ... : 0, nn:204) is
+        // staged as all zeros and adds nothing
+        const bool filled = start && pos >= 0;
+        const unsigned fills = __ballot_sync(kFull, filled);
+        if (filled) {
           const unsigned later = starts & ~((2u << lane) - 1u);
           const int e = later ? (__ffs(later) - 1) : endlane;
           const float cnt = (float)(e - lane);
           const float4 vv = __ldg(a.snap.vel + pos);
           const float vlos = fmaf(uz, vv.z, fmaf(uy, vv.y, ux * vv.x));
+          float4* dst = runs[w][__popc(fills & ((1u << lane) - 1u))];
 #pragma unroll
           for (int l = 0; l < NL; ++l) {
             if (lon[l]) {
               const float2 pw = __ldg(ew[l] + pos);
               const float sc = __fdividef(2.0f, pw.y);  // exp(-4 ln2 (d/w)^2) = 2^(-(2d/w)^2)
-              rpk[l] = pw.x * cnt;
-              rsc[l] = sc;
-              rns[l] = -(vlos * shk[l]) * sc;
+              dst[l] = pw.x != 0.0f ? make_float4(pw.x * cnt, sc, -(vlos * shk[l]) * sc, 0.0f)
+                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             }
           }
         }
-        unsigned todo = starts;
-        while (todo) {
-          const int s = __ffs(todo) - 1;
-          todo &= todo - 1;
+        __syncwarp();
+        const int nruns = __popc(fills);
+        for (int q0 = 0; q0 < nruns; ++q0) {
 #pragma unroll
           for (int l = 0; l < NL; ++l) {
             if (lon[l]) {
-              const float pk = __shfl_sync(kFull, rpk[l], s);
-              if (pk != 0.0f) {  // intpolpeak ? ... : 0 (nn:204); no neighbour -> 0
-                const float sc = __shfl_sync(kFull, rsc[l], s);
-                const float ns = __shfl_sync(kFull, rns[l], s);
+              const float4 t = runs[w][q0][l];  // same address in every lane: one broadcast load
+              {
 #pragma unroll
                 for (int m = 0; m < NB; ++m) {
                   if (m < nw[l]) {
-                    const float q = fmaf(lam[l][m], sc, ns);
-                    part[l][m] = fmaf(pk, ex2_approx(-q * q), part[l][m]);
+                    const float q = fmaf(lam[l][m], t.y, t.z);
+                    part[l][m] = fmaf(t.x, ex2_approx(-q * q), part[l][m]);
                   }
                 }
               }
             }
           }
         }
+        __syncwarp();  // the run list is rewritten by the next chunk
 #pragma unroll
         for (int l = 0; l < NL; ++l)
 #pragma unroll
