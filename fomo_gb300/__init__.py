@@ -92,7 +92,8 @@ SIGNATURES = {
                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_int,
                             ctypes.c_char_p, ctypes.c_int],
     "fomo_emission": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, _F, _F],
-    "fomo_render": [ctypes.c_void_p, ctypes.POINTER(Request), _F, _I32, ctypes.POINTER(ViewInfo)],
+    "fomo_thomson_emission": [ctypes.c_void_p, ctypes.c_int, _F, _F],
+    "fomo_render":[ctypes.c_void_p, ctypes.POINTER(Request), _F, _I32, ctypes.POINTER(ViewInfo)],
     "fomo_render_device": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_void_p, ctypes.c_void_p,
                            ctypes.POINTER(ViewInfo), ctypes.c_void_p],
     "fomo_render_noalloc": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_void_p, ctypes.c_void_p],
@@ -224,6 +225,15 @@ class Context:
         w = np.empty(n, np.float32)
         self._check(self._L.fomo_emission(self.h, sid, tid, int(imaging), abundratio, _fp(eps), _fp(w)))
         return eps, w
+
+    def thomson_emission(self, sid: int, n: int | None = None):
+        """Per-point (n*tot, n*pol) Thomson terms in the snapshot's original point order."""
+        if n is None:
+            n = self.snapshot_info(sid).npoints
+        tot = np.empty(n, np.float32)
+        pol = np.empty(n, np.float32)
+        self._check(self._L.fomo_thomson_emission(self.h, sid, _fp(tot), _fp(pol)))
+        return tot, pol
 
     # -- rendering
     @staticmethod

@@ -1204,6 +1204,26 @@ int fomo_emission(fomo_ctx* ctx, int snapshot, int table, int imaging, double ab
   return FOMO_OK;
 }
 
+int fomo_thomson_emission(fomo_ctx* ctx, int snapshot, float* tot, float* pol) {
+  if (!ctx || !tot || !pol) return FOMO_EINVAL;
+  cudaSetDevice(ctx->device);
+  auto sit = ctx->snaps.find(snapshot);
+  if (sit == ctx->snaps.end()) return set_err(ctx, FOMO_ENOTFOUND, "unknown snapshot id");
+  const float2* tp = nullptr;
+  int rc = get_thomson_payload(ctx, sit->second, &tp);
+  if (rc) return rc;
+  const int64_t n = sit->second.n;
+  rc = ctx->out_arena.reserve(ctx, sizeof(float) * 2 * (size_t)n);
+  if (rc) return rc;
+  float* a = reinterpret_cast<float*>(ctx->out_arena.base);
+  float* b = a + n;
+  FOMO_CUDA(launch_unsort_payload(sit->second.pts, tp, n, a, b, ctx->stream), "Thomson unsort");
+  FOMO_CUDA(cudaMemcpyAsync(tot, a, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream), "Thomson download");
+  FOMO_CUDA(cudaMemcpyAsync(pol, b, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream), "Thomson download");
+  FOMO_CUDA(cudaStreamSynchronize(ctx->stream), "Thomson emission");
+  return FOMO_OK;
+}
+
 int fomo_set_march_config(fomo_ctx* ctx, int tile_w, int tile_h, int blocks_per_sm) {
   if (!ctx || tile_w < 0 || tile_h < 0 || blocks_per_sm < 0) return FOMO_EINVAL;
   if ((tile_w == 0) != (tile_h == 0)) return set_err(ctx, FOMO_EINVAL, "set both tile dimensions or neither");

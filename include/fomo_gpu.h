@@ -117,6 +117,12 @@ int fomo_table_get_info(fomo_ctx* ctx, int id, double* lambda0, double* atweight
  * FoMo::Imaging.  Computed on the device (and cached for later renders). */
 int fomo_emission(fomo_ctx* ctx, int snapshot, int table, int imaging, double abundratio, float* eps, float* fwhm);
 
+/* Per-point Thomson scattering terms of a snapshot, in its original point
+ * order: tot = n * total term, pol = n * polarised term, the GoftCube vars
+ * that thomsonfromdatacube returns (fomo-thomson.cpp:60-92).  Computed on the
+ * device (and cached for later Thomson renders). */
+int fomo_thomson_emission(fomo_ctx* ctx, int snapshot, float* tot, float* pol);
+
 /* ---- one render request: the arguments of RenderWithNearestNeighbour /
  * RenderWithThomson (FoMo-internal.h:23-27) for one (l, b) view. */
 typedef struct {

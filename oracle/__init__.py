@@ -229,3 +229,14 @@ def ref_render(method: str, snap, table_path: str, l, b, nx, ny, nz, L, lambda_w
     if rc != 0:
         raise RuntimeError(ref().ref_last_error().decode())
     return out, (gx, gy, gl), meta
+
+
+def ref_render_and_write(method: str, snap, table_path: str, l, b, nx, ny, nz, L, lambda_width, options: int,
+                         out_path: str):
+    """FoMoObject::render(l, b) of the reference, then RenderCube::writegoftcube(out_path)
+    with the write-option bits `options` (bit 0 binary .dat, bit 1 text .txt)."""
+    rc = ref().ref_render_and_write(method.encode(), ctypes.c_long(snap.npoints), *[_fp(a) for a in snap.arrays()],
+                                    (table_path or "").encode(), ctypes.c_double(l), ctypes.c_double(b), nx, ny, nz, L,
+                                    ctypes.c_double(lambda_width), int(options), out_path.encode())
+    if rc != 0:
+        raise RuntimeError(ref().ref_last_error().decode())

@@ -11,6 +11,9 @@ synthetic cases and stores inputs and outputs as compressed .npz files:
     nn_edges.npz     ragged sizes, nz = 1, empty corners, out-of-table points
     thomson.npz      Thomson (pB) views
     nn_medium.npz    a larger spectroscopic case (24^3 points, 32x32x48, L = 32)
+    writer_*.txt/.dat the reference's own text and binary output files of three
+                     small renders (spectroscopic, DN imaging, Thomson), with
+                     their inputs in writers.npz
 
 Run from the repository root:  python tests/golden/make_golden.py
 The fixtures are committed; the GPU machine has no reference tree and only reads them.
@@ -112,6 +115,30 @@ def main():
         d = _render_cases("NearestNeighbour", sm, t, [(0.7, 0.5)], 32, 32, 48, 32, 0.6, tmp)
         np.savez_compressed(os.path.join(HERE, "nn_medium.npz"), eps=eps, fwhm=w, **_snap_dict(sm),
                             **_table_dict(t), **d, **info)
+
+        # 6. on-disk formats: the reference's RenderCube::writegoftcube (text and
+        #    binary) of three small renders; table paths are relative so the
+        #    file headers do not depend on where this ran
+        cwd = os.getcwd()
+        os.chdir(tmp)
+        try:
+            synth.write_table(t, "table.dat")
+            synth.write_table(bt, "band.dat")
+            ws = synth.loop_snapshot(9, seed=5)
+            wt = synth.thomson_snapshot(9)
+            oracle.ref_render_and_write("NearestNeighbour", ws, "table.dat", 0.3, 0.2, 8, 6, 10, 8, 0.6, 3, "w_nn.txt")
+            oracle.ref_render_and_write("NearestNeighbour", ws, "band.dat", 0.4, -0.3, 7, 5, 10, 1, 1e5, 3,
+                                        "w_img.txt")
+            oracle.ref_render_and_write("Thomson", wt, "", 0.2, 0.3, 8, 6, 12, 1, 1e5, 3, "w_th.txt")
+            for f in ("w_nn", "w_img", "w_th"):
+                for ext in (".txt", ".dat"):
+                    with open(f + ext, "rb") as src, open(os.path.join(HERE, "writer_" + f[2:] + ext), "wb") as dst:
+                        dst.write(src.read())
+        finally:
+            os.chdir(cwd)
+        np.savez_compressed(os.path.join(HERE, "writers.npz"), **{"nn_" + k: v for k, v in _snap_dict(ws).items()},
+                            **{"th_" + k: v for k, v in _snap_dict(wt).items()}, **_table_dict(t),
+                            **_table_dict(bt, "band"), **info)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

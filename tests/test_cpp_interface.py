@@ -1,0 +1,206 @@
+"""The C++ object interface (include/FoMo.h) as a FoMo-C user sees it.
+
+CPU: the reader and writers reproduce the reference's own output files
+byte for byte (tests/golden/writer_*, written by the reference's
+RenderCube::writegoftcube, fomo-io.cpp:26-150), the gzip option produces
+readable .gz files, and a user program in the style of the reference's
+example (fomo-c/example/example.cpp) compiles, links and -- without a GPU --
+fails loudly instead of falling back to a CPU path.
+
+GPU: that program renders the golden cases through FoMoObject::render and its
+files match the reference's: same header, same image grid (bit for bit), the
+intensities within the render tolerance.
+"""
+
+import gzip
+import os
+import shutil
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+import fomo_gb300 as fg
+from tests import _golden as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden")
+TOL = 1e-4  # normalised max error of a rendered cube
+
+
+def read_cube(path):
+    """Parse a FoMo cube file (.txt or .dat, optionally .gz) into a dict."""
+    raw = open(path, "rb").read()
+    if path.endswith(".gz"):
+        raw = gzip.decompress(raw)
+    stem = path[:-3] if path.endswith(".gz") else path
+    if stem.endswith(".dat"):
+        end = raw.index(b"#")
+        version = raw[:end].decode()
+        off = end + 1
+        dim, ng, nvars = struct.unpack_from("<iii", raw, off)
+        off += 12
+
+        def string():
+            nonlocal off
+            (n,) = struct.unpack_from("<q", raw, off)
+            off += 8
+            s = raw[off:off + n].decode()
+            off += n
+            return s
+
+        units = [string() for _ in range(dim + nvars)]
+        chianti, abund = string(), string()
+        cols = np.frombuffer(raw, np.float32, (dim + nvars) * ng, off).reshape(dim + nvars, ng)
+        return dict(version=version, dim=dim, ng=ng, nvars=nvars, units=units, chianti=chianti, abund=abund,
+                    data=cols.T.copy(), body=raw[end:])
+    lines = raw.decode().split("\n")
+    dim, ng, nvars = int(lines[1]), int(lines[2]), int(lines[3])
+    units = lines[4].split("\t")[:dim + nvars]
+    rows = [list(map(float, ln.split())) for ln in lines[7:7 + ng]]
+    return dict(version=lines[0], dim=dim, ng=ng, nvars=nvars, units=units, chianti=lines[5], abund=lines[6],
+                data=np.array(rows, np.float64).reshape(ng, dim + nvars), body="\n".join(lines[1:]).encode())
+
+
+@pytest.fixture(scope="module")
+def programs(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    if not os.path.exists(fg.LIB_PATH):
+        from fomo_gb300 import build
+        build.build()
+    out = tmp_path_factory.mktemp("cpp")
+    libdir = os.path.dirname(fg.LIB_PATH)
+    progs = {}
+    for name in ("example_render", "roundtrip_cube"):
+        exe = str(out / name)
+        cmd = ["g++", "-std=c++11", "-O1", "-I", os.path.join(ROOT, "include"),
+               os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-L", libdir, "-lfomo_gpu",
+               "-Wl,-rpath," + libdir, "-o", exe]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        progs[name] = exe
+    return progs
+
+
+# ---------------------------------------------------------------- CPU
+
+@pytest.mark.parametrize("case", ["nn", "img", "th"])
+def test_writers_reproduce_the_reference_files(programs, tmp_path, case):
+    src = os.path.join(GOLD, f"writer_{case}.dat")
+    out = str(tmp_path / "copy.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, "3"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for ext in (".dat", ".txt"):
+        ours, ref = read_cube(str(tmp_path / ("copy" + ext))), read_cube(os.path.join(GOLD, f"writer_{case}{ext}"))
+        assert ours["version"].startswith("FoMo-v") and ref["version"].startswith("FoMo-v")
+        assert ours["body"] == ref["body"], ext  # everything after the version string
+
+
+def test_reader_accepts_the_reference_text_format(programs, tmp_path):
+    src = os.path.join(GOLD, "writer_nn.txt")
+    out = str(tmp_path / "fromtext.dat")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, "1"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ours, ref = read_cube(out), read_cube(os.path.join(GOLD, "writer_nn.dat"))
+    assert (ours["dim"], ours["ng"], ours["nvars"]) == (ref["dim"], ref["ng"], ref["nvars"])
+    assert ours["units"] == ref["units"] and ours["chianti"] == ref["chianti"]
+    np.testing.assert_allclose(ours["data"], ref["data"], rtol=1e-7, atol=0)
+
+
+def test_gzip_option_and_delete_option(programs, tmp_path):
+    src = os.path.join(GOLD, "writer_img.dat")
+    out = str(tmp_path / "z.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, str(0b0111)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for ext in (".dat", ".txt"):
+        plain = open(str(tmp_path / ("z" + ext)), "rb").read()
+        assert gzip.decompress(open(str(tmp_path / ("z" + ext + ".gz")), "rb").read()) == plain
+    out2 = str(tmp_path / "d.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, out2, str(0b1111)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert not os.path.exists(str(tmp_path / "d.dat")) and not os.path.exists(str(tmp_path / "d.txt"))
+    assert read_cube(str(tmp_path / "d.dat.gz"))["body"] == read_cube(src)["body"]
+
+
+def _write_data(path, snap):
+    cols = np.stack([snap.x, snap.y, snap.z, snap.n, snap.T, snap.vx, snap.vy, snap.vz], axis=1)
+    with open(path, "w") as f:
+        for row in cols:
+            f.write(" ".join("%.9g" % v for v in row) + "\n")
+
+
+def test_example_program_fails_loudly_without_a_gpu(programs, tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from fomo_gb300 import synth
+    data = str(tmp_path / "points.txt")
+    _write_data(data, synth.loop_snapshot(4))
+    synth.write_table(synth.line_table(), str(tmp_path / "table.dat"))
+    r = subprocess.run([programs["example_render"], data, "table.dat", "NearestNeighbour", "0.1", "0.2", "8", "6",
+                        "10", "8", "0.6", str(tmp_path / "out.txt")], capture_output=True, text=True,
+                       cwd=str(tmp_path))
+    assert r.returncode == 2
+    assert "no usable CUDA device" in r.stderr
+    assert not os.path.exists(str(tmp_path / "out.txt"))
+
+
+def test_unknown_method_is_an_exception(programs, tmp_path):
+    from fomo_gb300 import synth
+    data = str(tmp_path / "points.txt")
+    _write_data(data, synth.loop_snapshot(3))
+    synth.write_table(synth.line_table(), str(tmp_path / "table.dat"))
+    r = subprocess.run([programs["example_render"], data, "table.dat", "NoSuchMethod", "0", "0", "8", "6", "10", "8",
+                        "0.6", str(tmp_path / "out.txt")], capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 2 and "unknown rendering method" in r.stderr
+
+
+# ---------------------------------------------------------------- GPU
+
+CASES = {
+    # name: (method, table key, l, b, nx, ny, nz, L, width)
+    "nn": ("NearestNeighbourGPU", "table", 0.3, 0.2, 8, 6, 10, 8, 0.6),
+    "img": ("NearestNeighbour", "band", 0.4, -0.3, 7, 5, 10, 1, 1e5),
+    "th": ("ThomsonGPU", None, 0.2, 0.3, 8, 6, 12, 1, 1e5),
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_example_program_matches_the_reference_files(programs, tmp_path, case):
+    method, tkey, l, b, nx, ny, nz, L, width = CASES[case]
+    z = G.load("writers.npz")
+    pre = "th_" if case == "th" else "nn_"
+    snap = G.snapshot({k[len(pre):]: v for k, v in z.items() if k.startswith(pre)})
+    data = str(tmp_path / "points.txt")
+    _write_data(data, snap)
+    table = ""
+    if tkey:
+        table = "table.dat" if tkey == "table" else "band.dat"
+        with open(str(tmp_path / table), "wb") as f:
+            f.write(bytes(z[f"{tkey}_text"]))
+    out = str(tmp_path / "out.txt")
+    r = subprocess.run([programs["example_render"], data, table, method, repr(l), repr(b), str(nx), str(ny), str(nz),
+                        str(L), repr(width), out, "3"], capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert f"points {nx * ny * L}" in r.stdout
+    assert f"method {method}" in r.stdout
+    for ext in (".dat", ".txt"):
+        ours = read_cube(str(tmp_path / ("out" + ext)))
+        ref = read_cube(os.path.join(GOLD, f"writer_{case}{ext}"))
+        for k in ("dim", "ng", "nvars", "units", "chianti", "abund"):
+            assert ours[k] == ref[k], (ext, k)
+        d = ours["dim"]
+        if ext == ".dat":
+            assert np.array_equal(ours["data"][:, :d], ref["data"][:, :d])  # the image grid, bit for bit
+        else:
+            np.testing.assert_allclose(ours["data"][:, :d], ref["data"][:, :d], rtol=1e-7)
+        assert G.norm_max_err(ours["data"][:, d:], ref["data"][:, d:]) <= TOL, ext
+    # render() itself wrote the view with the default write options (text only)
+    # three characters, zero-filled on the left as iostream pads: 17 -> "017", -5 -> "0-5"
+    deg = lambda a: ("%d" % int(round(a * 180.0 / np.pi))).rjust(3, "0")  # noqa: E731
+    view = tmp_path / ("view-l%sb%s.txt" % (deg(l), deg(b)))
+    assert view.exists(), sorted(os.listdir(str(tmp_path)))
+    assert not (tmp_path / (view.name[:-4] + ".dat")).exists()
