@@ -156,11 +156,30 @@ __device__ __forceinline__ void coop_ring_pass(const SnapDev& S, const BoxQ& q, 
   const int* c = R.c;
   const GridParams& g = S.g;
   const float h = g.h;
+  const float to[3] = {q.tx, q.ty, q.tz}, oo[3] = {g.ox, g.oy, g.oz};
+  // squared gap from the target to the centre cell's slab along each axis
+  // (the centre is the target's cell, clamped into the grid: the nearest
+  // slab along that axis, also for a target outside the grid)
+  float gc[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float gj = axis_gap(c[j], to[j], oo[j], h);
+    gc[j] = gj * gj;
+  }
   for (int s = 0;; ++s) {
     const float bound = EXACT ? band * (1.0f + kRelPrune) : gbest * (1.0f + kRelPrune);
-    if (s >= 2) {
-      const float lb = ((float)s - 1.0f - 2.0f * kCellMargin) * h;
-      if (lb * lb > bound) break;
+    if (s >= 1) {
+      // lower bound on the squared distance to any cell of ring s: one axis
+      // steps s cells away from the centre, the others stay at their nearest slab
+      float lb2 = FLT_MAX;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        float m = FLT_MAX;
+        if (c[j] - s >= b0[j]) m = axis_gap(c[j] - s, to[j], oo[j], h);
+        if (c[j] + s <= b1[j]) m = fminf(m, axis_gap(c[j] + s, to[j], oo[j], h));
+        if (m < FLT_MAX) lb2 = fminf(lb2, fmaf(m, m, gc[(j + 1) % 3] + gc[(j + 2) % 3]));
+      }
+      if (lb2 > bound) break;  // also when no axis has a cell left in the box
     }
     if (c[0] - s < b0[0] && c[0] + s > b1[0] && c[1] - s < b0[1] && c[1] + s > b1[1] && c[2] - s < b0[2] &&
         c[2] + s > b1[2])
