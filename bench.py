@@ -20,6 +20,10 @@ roofline   : the march kernel's algorithmic bytes / its event-timed duration
              against the measured HBM copy bandwidth.
 cpu_baseline: the oracle (C restatement, OpenMP on all host cores) on a bounded
              sample of rows of the plain configuration.
+serving    : a Poisson stream of mixed requests (200/s, 8 resident snapshots of
+             0.5M-8M points, random views, pixels, lambda bins and lines) through
+             the continuous-batching server: p50/p90/p99 latency, throughput,
+             and the same requests alone for comparison (N = 1 only).
 
 --impl reference runs the reference's CPU algorithm (the oracle port; the
 reference's own build needs Boost/GSL, absent on the GPU host) on a bounded
@@ -130,6 +134,82 @@ def algorithmic_bytes_per_sample(nlines, L, nz):
     # winning point's FP32 position (12 B) + v_los (4 B) + (eps, w) per line (8 B)
     # + the output cube written once per ray, spread over its LOS samples
     return 12 + 4 + 8 * nlines + 4.0 * L * nlines / nz
+
+
+SERVE_SNAPSHOT_POINTS = (524288, 1048576, 1572864, 2097152, 3145728, 4194304, 6291456, 8388608)
+SERVE_CHANNELS = (94, 131, 171, 193, 211, 335)
+SERVE_NZ = 256
+SERVE_MAX_CUBE = 1 << 22  # floats: larger (pixels, L) draws are redrawn (16 MB host result cap)
+
+
+def serving_leg(device, n_req=300, rate=200.0, seed=11):
+    """Mixed request stream through the continuous-batching server.
+
+    Eight resident flux-rope snapshots of 0.5M-8M points; Poisson arrivals at
+    `rate` per second (seeded); per request a random snapshot, view (l in
+    [0, 90 deg], b in [-20, 20 deg]), pixels in {64, 128, 256, 512, 1024}^2 and
+    L in {1, 16, 64, 128} (L = 1 renders one of six broadband DN channels,
+    otherwise one of four spectral lines), nz = 256.  Latency is submit ->
+    result in the caller's host buffer.  The same requests are then run alone,
+    one at a time, through the same server: their latency, their throughput,
+    and the largest difference between each cube alone and in the mix."""
+    import fomo_gb300 as fg
+    from fomo_gb300 import synth
+    rng = np.random.default_rng(seed)
+    with fg.Server(device) as srv:
+        ctx = srv.ctx
+        sids = [ctx.snapshot(synth.flux_rope_snapshot(n, seed=20 + k)) for k, n in enumerate(SERVE_SNAPSHOT_POINTS)]
+        line_t = [ctx.table(synth.line_table(peak_logT=p, lambda0=lam, ion=ion)) for p, lam, ion in LINES]
+        band_t = [ctx.table(synth.broadband_table(c, peak_logT=5.8 + 0.15 * k)) for k, c in enumerate(SERVE_CHANNELS)]
+        reqs = []
+        while len(reqs) < n_req:
+            npx = int(rng.choice([64, 128, 256, 512, 1024]))
+            L = int(rng.choice([1, 16, 64, 128]))
+            if npx * npx * L > SERVE_MAX_CUBE:
+                continue
+            sid = sids[int(rng.integers(len(sids)))]
+            tid = band_t[int(rng.integers(len(band_t)))] if L == 1 else line_t[int(rng.integers(len(line_t)))]
+            reqs.append(ctx.request(sid, tid, fg.METHOD_NN, npx, npx, SERVE_NZ, L, float(rng.uniform(0, math.pi / 2)),
+                                    float(rng.uniform(-math.pi / 9, math.pi / 9)), WIDTH))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+        # warm-up: every (snapshot, table) pair's emissivity, computed once and kept resident
+        pairs = sorted({(q.snapshot, q.table, q.nlambda == 1) for q in reqs})
+        for sid, tid, img in pairs:
+            q = ctx.request(sid, tid, fg.METHOD_NN, 8, 8, 8, 1 if img else 16, 0.1, 0.1, WIDTH)
+            buf = np.empty(8 * 8 * q.nlambda, np.float32)
+            srv.wait(srv.submit(q, buf))
+        elems = [q.nx * q.ny * q.nlambda for q in reqs]
+        outs = [np.empty(e, np.float32) for e in elems]
+        t0 = time.perf_counter()
+        tickets = []
+        for i, q in enumerate(reqs):
+            delay = arrivals[i] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append(srv.submit(q, outs[i]))
+        st = [srv.wait(t, timeout=900.0) for t in tickets]
+        lat = np.array([s.t_done - s.t_submit for s in st]) * 1e3
+        span = max(s.t_done for s in st) - min(s.t_submit for s in st)
+        samples = float(sum(q.nx * q.ny * q.nz for q in reqs))
+        # the same requests alone, one at a time
+        alone_lat, worst = [], 0.0
+        t1 = time.perf_counter()
+        for i, q in enumerate(reqs):
+            a = np.empty(elems[i], np.float32)
+            s = srv.wait(srv.submit(q, a), timeout=900.0)
+            alone_lat.append((s.t_done - s.t_submit) * 1e3)
+            den = float(np.abs(a).max())
+            if den > 0:
+                worst = max(worst, float(np.abs(a - outs[i]).max()) / den)
+        alone_s = time.perf_counter() - t1
+    return {"requests": n_req, "arrival_rate_hz": rate, "arrivals": "Poisson, seeded",
+            "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()), "span_s": float(span),
+            "line_samples_per_s": samples / span,
+            "alone_p50_ms": float(np.percentile(alone_lat, 50)), "alone_p99_ms": float(np.percentile(alone_lat, 99)),
+            "alone_line_samples_per_s": samples / alone_s, "mix_vs_alone_max_norm_err": worst,
+            "snapshots_points": list(SERVE_SNAPSHOT_POINTS), "nz": SERVE_NZ,
+            "mix": "pixels {64..1024}^2 x L {1,16,64,128} (cube <= 16 MB), 4 lines / 6 DN channels, random views"}
 
 
 def cpu_baseline_sample(target_s=10.0):
@@ -317,6 +397,12 @@ def run_ours(args):
         except Exception:
             traffic = None
 
+    serving = None
+    if rank == 0 and world == 1 and not args.no_serving:
+        ctx.close()  # the server leg builds its own context and snapshots
+        ctx = None
+        serving = serving_leg(local)
+
     if rank == 0:
         cpu = cpu_baseline_sample() if not args.no_cpu else None
         out = {
@@ -344,9 +430,11 @@ def run_ours(args):
             "clocks": clk.summary(),
             # per step: view init, view extents, view finalize, first-pass march, deferred march
             "gpu_launches": 5 * args.steps,
+            "serving": serving,
         }
         print(json.dumps(out))
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     if dist:
         dist.destroy_process_group()
 
@@ -396,6 +484,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving (mixed request stream) leg")
     ap.add_argument("--profile-case", action="store_true", help="small direct-launch case for ncu captures")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -306,23 +306,36 @@ class Server:
         if rc != OK:
             raise FomoError(rc, "fomo_server_create failed")
         self.h = h
+        self._outs = {}  # ticket -> the caller's result array, alive until wait()
         # the server's own context, for resident snapshots and tables
         self.ctx = Context.__new__(Context)
         self.ctx._L = self._L
         self.ctx.h = ctypes.c_void_p(self._L.fomo_server_context(h))
 
     def submit(self, req: Request, out: np.ndarray) -> int:
+        """Queue a request; the result is written into `out` (float32, C-contiguous,
+        at least the cube's size) when it completes.  `out` is kept alive here
+        until wait() returns for the ticket."""
+        if out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise FomoError(EINVAL, "out must be a C-contiguous float32 array")
+        L = 1 if req.method == METHOD_THOMSON else req.nlambda
+        if out.size < req.nx * req.ny * L:
+            raise FomoError(EINVAL, f"out holds {out.size} floats, the cube needs {req.nx * req.ny * L}")
         t = ctypes.c_uint64()
         rc = self._L.fomo_server_submit(self.h, ctypes.byref(req), _fp(out), ctypes.byref(t))
         if rc != OK:
             raise FomoError(rc, self._L.fomo_server_last_error(self.h).decode())
+        self._outs[t.value] = out
         return t.value
 
     def wait(self, ticket: int, timeout: float = 120.0) -> RequestStats:
         st = RequestStats()
         rc = self._L.fomo_server_wait(self.h, ticket, timeout, ctypes.byref(st))
         if rc != OK:
+            if rc != ETIMEOUT:
+                self._outs.pop(ticket, None)
             raise FomoError(rc, self._L.fomo_server_last_error(self.h).decode())
+        self._outs.pop(ticket, None)
         return st
 
     def cancel(self, ticket: int):
@@ -332,9 +345,10 @@ class Server:
 
     def close(self):
         if self.h:
-            self._L.fomo_server_destroy(self.h)
+            self._L.fomo_server_destroy(self.h)  # finishes or cancels what is in flight
             self.h = None
             self.ctx.h = None
+            self._outs.clear()
 
     def __enter__(self):
         return self

@@ -98,8 +98,11 @@ def test_server_admission_rejects_oversized_request():
         tid = srv.ctx.table(synth.line_table())
         big = fg.Context.request(sid, tid, fg.METHOD_NN, 1024, 1024, 64, 128, 0.0, 0.0, 1e5)  # 512 MB cube
         with pytest.raises(fg.FomoError) as ei:
-            srv.submit(big, np.empty(1, np.float32))
+            srv.submit(big, np.empty(1024 * 1024 * 128, np.float32))  # never touched: rejected at submit
         assert ei.value.code == fg.EADMISSION
+        with pytest.raises(fg.FomoError) as ei:
+            srv.submit(big, np.empty(1, np.float32))  # a result array smaller than the cube
+        assert ei.value.code == fg.EINVAL
         ok = fg.Context.request(sid, tid, fg.METHOD_NN, 16, 16, 16, 16, 0.0, 0.0, 1e5)
         out = np.empty((16, 16, 16), np.float32)
         assert srv.wait(srv.submit(ok, out)).status == fg.OK
