@@ -14,9 +14,9 @@
 //     cells the segment passes near; the rows' point ranges are prefix-summed
 //     across the warp and loaded 32 points per round (balanced), and points
 //     within R are compacted into a per-warp shared-memory list with the index
-//     of the sample they project onto.  R = min(sqrt(3) * maxdistance,
-//     1.15 local point spacings), the local spacing estimated from the cells the
-//     segment crosses;
+//     of the sample they project onto.  R = min(sqrt(3) * maxdistance, the
+//     local point spacing), the spacing estimated from the occupancy of the
+//     cells the segment crosses;
 //  2. bucket sort: the list is counting-sorted by that sample index;
 //  3. scan: each sample tests the candidates of the buckets within R of it:
 //     FP32 squared distance, and the Chebyshev distance against maxdistance
@@ -28,10 +28,11 @@
 //     the points' bounding box or inside the covered ball.  Near-ties (two best
 //     FP32 distances within 4e-6) are re-ranked with the exact FP64 distance in
 //     Boost's order (dz^2 + (dy^2 + dx^2)) and the lowest original index;
-//  5. fallback: every other sample (about 1 %) is resolved by the whole warp
-//     together: rings of grid cells around the sample's cell, clipped to its
-//     box (corners rounded from FP64 as the reference does), rows flattened
-//     across the lanes, stopped by a conservative distance bound, warp argmin.
+//  5. defer: every other sample (about 1 %) contributes nothing here; its
+//     segment is recorded, and a second kernel (march_deferred) searches each
+//     such sample on one lane -- rings of grid cells around the sample's cell,
+//     clipped to its box (corners rounded from FP64 as the reference does),
+//     nearest ring first, stopped by a distance bound -- then adds its emission.
 // Either way the chosen neighbour is the FP64 argmin strictly inside the box.
 //
 // Spectroscopic mode: equal neighbours of consecutive samples are merged into
@@ -42,8 +43,8 @@
 // Gaussian can exceed 2^-64 of its peak; the others are written as 0) in a
 // per-chunk FP32 partial, folded into the per-ray sum with Kahan compensation.
 // Imaging (L = 1) and Thomson (pB) add per-sample values through a warp
-// reduction.  One warp owns one ray: no atomics on the output; results are
-// deterministic and independent of what else shares the launch.
+// reduction.  One warp owns one ray in the first pass (no atomics); the
+// deferred samples' emission is added with atomics afterwards.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
@@ -64,16 +65,15 @@ constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
 constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
 constexpr int kSegCap = 256;          // candidates per segment
-constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule before the cooperative fallback
+constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule beyond which it is deferred
 constexpr float kRScale = 1.0f;       // gather radius in local point spacings
 
-constexpr int kUnionCap = 2 * kSegCap;  // points of the union-of-boxes list of a segment's fallback samples
 
 struct __align__(16) SegSmem {
   // [0, kSegCap): gathered candidates; [kSegCap, 2 kSegCap): the same sorted by
-  // the sample they project onto.  The union-of-boxes list uses all of it.
-  float4 q[kUnionCap];
-  int pos[kUnionCap];
+  // the sample they project onto
+  float4 q[2 * kSegCap];
+  int pos[2 * kSegCap];
   int bstart[kSeg + 1];
   int cursor[kSeg];
   unsigned char cb[kSegCap];
@@ -81,24 +81,6 @@ struct __align__(16) SegSmem {
 
 struct BoxQ {
   float tx, ty, tz, lox, loy, loz, hix, hiy, hiz;
-};
-
-__device__ __forceinline__ BoxQ shfl_box(const BoxQ& b, int src) {
-  BoxQ q;
-  q.tx = __shfl_sync(0xffffffffu, b.tx, src);
-  q.ty = __shfl_sync(0xffffffffu, b.ty, src);
-  q.tz = __shfl_sync(0xffffffffu, b.tz, src);
-  q.lox = __shfl_sync(0xffffffffu, b.lox, src);
-  q.loy = __shfl_sync(0xffffffffu, b.loy, src);
-  q.loz = __shfl_sync(0xffffffffu, b.loz, src);
-  q.hix = __shfl_sync(0xffffffffu, b.hix, src);
-  q.hiy = __shfl_sync(0xffffffffu, b.hiy, src);
-  q.hiz = __shfl_sync(0xffffffffu, b.hiz, src);
-  return q;
-}
-
-struct CellRange {
-  int b0[3], b1[3], c[3];
 };
 
 __device__ __forceinline__ float axis_gap(int c, float t, float o, float h) {
@@ -142,249 +124,6 @@ __device__ __forceinline__ int warp_owner(int incl, int i) {
 }
 
 // ---------------------------------------------------------------------------
-// Cooperative exact search for one sample (the fallback path).  All lanes
-// hold the same box; the rings of cells around the target's cell are walked
-// together, each ring's rows flattened across the lanes.
-// ---------------------------------------------------------------------------
-template <bool EXACT>
-__device__ __forceinline__ void coop_ring_pass(const SnapDev& S, const BoxQ& q, const CellRange& R, float& gbest,
-                                               float band, float& lb1, float& lb2, int& lpos, int& lorig,
-                                               double& lD, int& lDorig, int& lDpos) {
-  const int lane = threadIdx.x & 31;
-  const int* b0 = R.b0;
-  const int* b1 = R.b1;
-  const int* c = R.c;
-  const GridParams& g = S.g;
-  const float h = g.h;
-  const float to[3] = {q.tx, q.ty, q.tz}, oo[3] = {g.ox, g.oy, g.oz};
-  // squared gap from the target to the centre cell's slab along each axis
-  // (the centre is the target's cell, clamped into the grid: the nearest
-  // slab along that axis, also for a target outside the grid)
-  float gc[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const float gj = axis_gap(c[j], to[j], oo[j], h);
-    gc[j] = gj * gj;
-  }
-  for (int s = 0;; ++s) {
-    const float bound = EXACT ? band * (1.0f + kRelPrune) : gbest * (1.0f + kRelPrune);
-    if (s >= 1) {
-      // lower bound on the squared distance to any cell of ring s: one axis
-      // steps s cells away from the centre, the others stay at their nearest slab
-      float lb2 = FLT_MAX;
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        float m = FLT_MAX;
-        if (c[j] - s >= b0[j]) m = axis_gap(c[j] - s, to[j], oo[j], h);
-        if (c[j] + s <= b1[j]) m = fminf(m, axis_gap(c[j] + s, to[j], oo[j], h));
-        if (m < FLT_MAX) lb2 = fminf(lb2, fmaf(m, m, gc[(j + 1) % 3] + gc[(j + 2) % 3]));
-      }
-      if (lb2 > bound) break;  // also when no axis has a cell left in the box
-    }
-    if (c[0] - s < b0[0] && c[0] + s > b1[0] && c[1] - s < b0[1] && c[1] + s > b1[1] && c[2] - s < b0[2] &&
-        c[2] + s > b1[2])
-      break;
-    const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
-    const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
-    const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
-    for (int rb = 0; rb < nrows; rb += 32) {
-      const int rr = rb + lane;
-      int baseA = 0, nA = 0, baseB = 0, nB = 0;
-      if (rr < nrows) {
-        const int kz = z0 + rr / nyr, jy = y0 + rr % nyr;
-        const bool onz = (kz == c[2] - s) || (kz == c[2] + s);
-        const bool ony = (jy == c[1] - s) || (jy == c[1] + s);
-        const float gz = axis_gap(kz, q.tz, g.oz, h), gy = axis_gap(jy, q.ty, g.oy, h);
-        const float gyz = fmaf(gy, gy, gz * gz);
-        if (gyz <= bound) {
-          const int rowbase = (kz * g.dy + jy) * g.dx;
-          if (onz || ony) {
-            int x0 = max(c[0] - s, b0[0]), x1 = min(c[0] + s, b1[0]);
-            if (bound < FLT_MAX) {
-              // clip the row to cells within sqrt(bound - gyz) of the target in x
-              const float rem = fmaxf(bound - gyz, 0.0f);
-              const float rx = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
-              x0 = max(x0, cell_coord(q.tx - rx, g.ox, g.inv_h, g.dx));
-              x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
-            }
-            if (x0 <= x1) {
-              baseA = __ldg(S.cell_start + rowbase + x0);
-              nA = __ldg(S.cell_start + rowbase + x1 + 1) - baseA;
-            }
-          } else {
-            const int xl = c[0] - s, xr = c[0] + s;
-            if (xl >= b0[0]) {
-              const float gx = axis_gap(xl, q.tx, g.ox, h);
-              if (fmaf(gx, gx, gyz) <= bound) {
-                baseA = __ldg(S.cell_start + rowbase + xl);
-                nA = __ldg(S.cell_start + rowbase + xl + 1) - baseA;
-              }
-            }
-            if (s > 0 && xr <= b1[0]) {
-              const float gx = axis_gap(xr, q.tx, g.ox, h);
-              if (fmaf(gx, gx, gyz) <= bound) {
-                baseB = __ldg(S.cell_start + rowbase + xr);
-                nB = __ldg(S.cell_start + rowbase + xr + 1) - baseB;
-              }
-            }
-          }
-        }
-      }
-      const int tot = nA + nB;
-      const int incl = warp_incl_scan(tot);
-      const int excl = incl - tot;
-      const int total = __shfl_sync(kFull, incl, 31);
-      for (int ib = 0; ib < total; ib += 32) {
-        const int i = ib + lane;
-        const int own = warp_owner(incl, i);
-        const int oA = __shfl_sync(kFull, baseA, own), onA = __shfl_sync(kFull, nA, own);
-        const int oB = __shfl_sync(kFull, baseB, own), oe = __shfl_sync(kFull, excl, own);
-        if (i < total) {
-          const int w = i - oe;
-          const int p = (w < onA) ? oA + w : oB + (w - onA);
-          const float4 v = __ldg(S.pts + p);
-          if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-            const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-            const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            if (!EXACT) {
-              if (d < lb1) {
-                lb2 = lb1;
-                lb1 = d;
-                lpos = p;
-                lorig = __float_as_int(v.w);
-              } else if (d < lb2) {
-                lb2 = d;
-              }
-            } else if (d <= band) {
-              const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
-              const int o = __float_as_int(v.w);
-              if (D < lD || (D == lD && o < lDorig)) {
-                lD = D;
-                lDorig = o;
-                lDpos = p;
-              }
-            }
-          }
-        }
-      }
-    }
-    if (!EXACT) gbest = warp_min(lb1);
-  }
-}
-
-// Nearest point strictly inside the box q (the same for all lanes); the
-// result is returned to every lane.
-__device__ __forceinline__ void coop_search(const SnapDev& S, const BoxQ& q, int* pos, int* orig) {
-  const GridParams& g = S.g;
-  *pos = -1;
-  *orig = -1;
-  if (!(q.lox < g.maxx && q.hix > g.minx && q.loy < g.maxy && q.hiy > g.miny && q.loz < g.maxz &&
-        q.hiz > g.minz && q.lox < q.hix && q.loy < q.hiy && q.loz < q.hiz))
-    return;
-  CellRange R;
-  R.b0[0] = cell_coord(q.lox, g.ox, g.inv_h, g.dx);
-  R.b1[0] = cell_coord(q.hix, g.ox, g.inv_h, g.dx);
-  R.b0[1] = cell_coord(q.loy, g.oy, g.inv_h, g.dy);
-  R.b1[1] = cell_coord(q.hiy, g.oy, g.inv_h, g.dy);
-  R.b0[2] = cell_coord(q.loz, g.oz, g.inv_h, g.dz);
-  R.b1[2] = cell_coord(q.hiz, g.oz, g.inv_h, g.dz);
-  R.c[0] = cell_coord(q.tx, g.ox, g.inv_h, g.dx);
-  R.c[1] = cell_coord(q.ty, g.oy, g.inv_h, g.dy);
-  R.c[2] = cell_coord(q.tz, g.oz, g.inv_h, g.dz);
-  float gbest = FLT_MAX, lb1 = FLT_MAX, lb2 = FLT_MAX;
-  int lpos = -1, lorig = -1, lDorig = 0x7fffffff, lDpos = -1;
-  double lD = DBL_MAX;
-  coop_ring_pass<false>(S, q, R, gbest, 0.0f, lb1, lb2, lpos, lorig, lD, lDorig, lDpos);
-  const float g1 = warp_min(lb1);
-  if (!(g1 < FLT_MAX)) return;
-  const unsigned at_g1 = __ballot_sync(kFull, lb1 == g1);
-  const float g2 = warp_min(lb1 == g1 ? lb2 : lb1);
-  if (__popc(at_g1) > 1 || g2 <= g1 * (1.0f + kRelTie)) {
-    // possible FP64 tie (also two lanes at the same FP32 minimum): exact
-    // re-rank of the contenders, lowest index wins
-    float fixed = g1;
-    coop_ring_pass<true>(S, q, R, fixed, g1 * (1.0f + kRelTie), lb1, lb2, lpos, lorig, lD, lDorig, lDpos);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double D2 = __shfl_xor_sync(kFull, lD, o);
-      const int o2 = __shfl_xor_sync(kFull, lDorig, o);
-      const int p2 = __shfl_xor_sync(kFull, lDpos, o);
-      if (D2 < lD || (D2 == lD && o2 < lDorig)) {
-        lD = D2;
-        lDorig = o2;
-        lDpos = p2;
-      }
-    }
-    *pos = lDpos;
-    *orig = lDorig;
-  } else {
-    const int w = __ffs(at_g1) - 1;
-    *pos = __shfl_sync(kFull, lpos, w);
-    *orig = __shfl_sync(kFull, lorig, w);
-  }
-}
-
-// Nearest point of the shared list lq[0, n) strictly inside the box q (the
-// same for all lanes), scanned by the whole warp; -1 when none.  Returns the
-// list slot to every lane.
-__device__ __forceinline__ int coop_list_search(const float4* lq, int n, const BoxQ& q) {
-  const int lane = threadIdx.x & 31;
-  float lb1 = FLT_MAX, lb2 = FLT_MAX;
-  int li = -1;
-  for (int c = lane; c < n; c += 32) {
-    const float4 v = lq[c];
-    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-      const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      if (d2 < lb1) {
-        lb2 = lb1;
-        lb1 = d2;
-        li = c;
-      } else if (d2 < lb2) {
-        lb2 = d2;
-      }
-    }
-  }
-  const float g1 = warp_min(lb1);
-  if (!(g1 < FLT_MAX)) return -1;
-  const unsigned at_g1 = __ballot_sync(kFull, lb1 == g1);
-  const float g2 = warp_min(lb1 == g1 ? lb2 : lb1);
-  if (__popc(at_g1) == 1 && g2 > g1 * (1.0f + kRelTie)) return __shfl_sync(kFull, li, __ffs(at_g1) - 1);
-  // possible FP64 tie: exact re-rank of the contenders, lowest original index wins
-  const float band = g1 * (1.0f + kRelTie);
-  double lD = DBL_MAX;
-  int lo = 0x7fffffff;
-  li = -1;
-  for (int c = lane; c < n; c += 32) {
-    const float4 v = lq[c];
-    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-      if (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) <= band) {
-        const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
-        const int o = __float_as_int(v.w);
-        if (D < lD || (D == lD && o < lo)) {
-          lD = D;
-          lo = o;
-          li = c;
-        }
-      }
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const double D2 = __shfl_xor_sync(kFull, lD, o);
-    const int o2 = __shfl_xor_sync(kFull, lo, o);
-    const int c2 = __shfl_xor_sync(kFull, li, o);
-    if (D2 < lD || (D2 == lD && o2 < lo)) {
-      lD = D2;
-      lo = o2;
-      li = c2;
-    }
-  }
-  return li;
-}
-
-// ---------------------------------------------------------------------------
 // Rays and segments
 // ---------------------------------------------------------------------------
 
@@ -406,7 +145,6 @@ __device__ __forceinline__ int find_view(const int64_t* off, int nviews, int64_t
   return lo;
 }
 
-// Next ray for this warp; false when the queue is drained.
 // The ray of work item `item` (views' rays in tile order); false for the
 // padding items of partial tiles.
 __device__ __forceinline__ bool ray_of_item(const MarchArgs& a, const double3* ktab, int ktab_stride,
@@ -790,119 +528,6 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
   }
 }
 
-// Warp-collective: nearest neighbours of the deferred samples s0 + lane
-// (mask f0) and s0 + 32 + lane (mask f1) of ray r.  The points of the union
-// of their exact boxes are gathered once, then every such sample in turn is
-// searched in that list by the whole warp; when the union holds too many
-// points, each sample is searched by a ring search of the grid instead.
-__device__ __forceinline__ void resolve_deferred(const SnapDev& S, const RayCtx& r, int s0, unsigned f0, unsigned f1,
-                                                 SegSmem& sm, int (&pos)[2], int (&orig)[2],
-                                                 unsigned long long* stats) {
-  const int lane = threadIdx.x & 31;
-  const GridParams& g = S.g;
-  const bool need0 = (f0 >> lane) & 1u, need1 = (f1 >> lane) & 1u;
-  {
-    BoxQ mb[2];
-    float ulx = FLT_MAX, uly = FLT_MAX, ulz = FLT_MAX, uhx = -FLT_MAX, uhy = -FLT_MAX, uhz = -FLT_MAX;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      mb[i] = BoxQ{};
-      if (i ? need1 : need0) {
-        mb[i] = exact_box(r, s0 + lane + 32 * i);
-        ulx = fminf(ulx, mb[i].lox);
-        uly = fminf(uly, mb[i].loy);
-        ulz = fminf(ulz, mb[i].loz);
-        uhx = fmaxf(uhx, mb[i].hix);
-        uhy = fmaxf(uhy, mb[i].hiy);
-        uhz = fmaxf(uhz, mb[i].hiz);
-      }
-    }
-    ulx = fmaxf(warp_min(ulx), g.minx);
-    uly = fmaxf(warp_min(uly), g.miny);
-    ulz = fmaxf(warp_min(ulz), g.minz);
-    uhx = fminf(-warp_min(-uhx), g.maxx);
-    uhy = fminf(-warp_min(-uhy), g.maxy);
-    uhz = fminf(-warp_min(-uhz), g.maxz);
-    bool ok = true;
-    int ucount = 0;
-    if (ulx <= uhx && uly <= uhy && ulz <= uhz) {
-      const int x0 = cell_coord(ulx, g.ox, g.inv_h, g.dx), x1 = cell_coord(uhx, g.ox, g.inv_h, g.dx);
-      const int y0 = cell_coord(uly, g.oy, g.inv_h, g.dy), y1 = cell_coord(uhy, g.oy, g.inv_h, g.dy);
-      const int z0 = cell_coord(ulz, g.oz, g.inv_h, g.dz), z1 = cell_coord(uhz, g.oz, g.inv_h, g.dz);
-      const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
-      const unsigned lt = (1u << lane) - 1u;
-      if (nrows > kMaxRows) ok = false;
-      for (int rb = 0; ok && rb < nrows; rb += 32) {
-        const int rr = rb + lane;
-        int n = 0, base = 0;
-        if (rr < nrows) {
-          const int rowbase = ((z0 + rr / nyr) * g.dy + (y0 + rr % nyr)) * g.dx;
-          base = __ldg(S.cell_start + rowbase + x0);
-          n = __ldg(S.cell_start + rowbase + x1 + 1) - base;
-        }
-        const int incl = warp_incl_scan(n);
-        const int excl = incl - n;
-        const int total = __shfl_sync(kFull, incl, 31);
-        for (int ib = 0; ib < total; ib += 32) {
-          const int i = ib + lane;
-          const int own = warp_owner(incl, i);
-          const int ob = __shfl_sync(kFull, base, own);
-          const int oe = __shfl_sync(kFull, excl, own);
-          bool keep = false;
-          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-          int p = 0;
-          if (i < total) {
-            p = ob + (i - oe);
-            q = __ldg(S.pts + p);
-            keep = q.x >= ulx && q.x <= uhx && q.y >= uly && q.y <= uhy && q.z >= ulz && q.z <= uhz;
-          }
-          const unsigned msk = __ballot_sync(kFull, keep);
-          if (keep) {
-            const int slot = ucount + __popc(msk & lt);
-            if (slot < kUnionCap) {
-              sm.q[slot] = q;
-              sm.pos[slot] = p;
-            }
-          }
-          ucount += __popc(msk);
-        }
-      }
-      if (ucount > kUnionCap) ok = false;
-    }
-    __syncwarp();
-    if (stats && ok && lane == 0) atomicAdd(stats + kStatFbUnion, (unsigned long long)(__popc(f0) + __popc(f1)));
-    // each deferred sample in turn, by the whole warp: a scan of the union
-    // list, or on overflow a ring search of the grid
-#pragma unroll 1
-    for (int i = 0; i < 2; ++i) {
-      unsigned fm = i ? f1 : f0;
-      while (fm) {
-        const int sl = __ffs(fm) - 1;
-        fm &= fm - 1;
-        const BoxQ q = shfl_box(i ? mb[1] : mb[0], sl);
-        int p, o;
-        if (ok) {
-          const int c = coop_list_search(sm.q, ucount, q);
-          p = c >= 0 ? sm.pos[c] : -1;
-          o = c >= 0 ? __float_as_int(sm.q[c].w) : -1;
-        } else {
-          coop_search(S, q, &p, &o);
-        }
-        if (lane == sl) {
-          if (i) {
-            pos[1] = p;
-            orig[1] = o;
-          } else {
-            pos[0] = p;
-            orig[0] = o;
-          }
-        }
-      }
-    }
-  }
-  __syncwarp();  // the list is rewritten by the next record
-}
-
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
@@ -1102,103 +727,267 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_imaging(MarchArgs a,
 // ---------------------------------------------------------------------------
 // Deferred samples: the march's first pass leaves about 1 % of the samples
 // (boxes reaching past its gather radius, mostly just outside the point
-// cloud) empty and records them.  This kernel finds their neighbours, writes
-// their NN indices and adds their emission to the rays' outputs, which the
-// march has already written (same stream, so after it).  One warp per record.
+// cloud, or segments whose capsule holds too many points) empty and records
+// them.  This kernel finds their neighbours, writes their NN indices and adds
+// their emission to the rays' outputs, which the march has already written
+// (same stream, so after it).  A warp takes 32 records at a time, flattens
+// their samples and gives every lane one sample to search on its own; the
+// contributions are then added per record, lane = lambda bin.
 // ---------------------------------------------------------------------------
 enum DeferredKind : int { kDeferredSpectral = 0, kDeferredImaging = 1, kDeferredThomson = 2 };
+constexpr int kDefBatch = 256;  // deferred samples staged per warp between search and contribution
 
-__global__ void __launch_bounds__(kThreads) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
+// Candidates p in [p0, p1) inside box q: the two best FP32 squared distances,
+// or (EXACT) the smallest FP64 distance within `band`, lowest original index
+// on exact ties.
+template <bool EXACT>
+__device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p0, int p1, float band, float& best,
+                                          float& second, int& bpos, int& borig, double& bD) {
+  for (int p = p0; p < p1; ++p) {
+    const float4 v = __ldg(S.pts + p);
+    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+      const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const int o = __float_as_int(v.w);
+      if (!EXACT) {
+        if (d < best) {
+          second = best;
+          best = d;
+          bpos = p;
+          borig = o;
+        } else if (d < second) {
+          second = d;
+        }
+      } else if (d <= band) {
+        const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
+        if (D < bD || (D == bD && o < borig)) {
+          bD = D;
+          borig = o;
+          bpos = p;
+        }
+      }
+    }
+  }
+}
+
+// One lane's walk over the rings of cells around the target's cell c (clamped
+// into the grid), nearest first.  A ring, a row or a cell is skipped when its
+// lower bound from the target exceeds the bound (the best squared distance so
+// far, or `band` in the EXACT pass); every loop is bounded by the box's cells.
+template <bool EXACT>
+__device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, const int (&b0)[3], const int (&b1)[3],
+                                           const int (&c)[3], const float (&gc)[3], float band, float& best,
+                                           float& second, int& bpos, int& borig, double& bD) {
+  const GridParams& g = S.g;
+  const float h = g.h;
+  const float to[3] = {q.tx, q.ty, q.tz}, oo[3] = {g.ox, g.oy, g.oz};
+  for (int s = 0;; ++s) {
+    if (c[0] - s < b0[0] && c[0] + s > b1[0] && c[1] - s < b0[1] && c[1] + s > b1[1] && c[2] - s < b0[2] &&
+        c[2] + s > b1[2])
+      break;  // no cell of this ring lies in the box
+    if (s >= 1) {
+      // one axis steps s cells from the centre, the others stay at their nearest slab
+      const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
+      float lb2 = FLT_MAX;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        float m = FLT_MAX;
+        if (c[j] - s >= b0[j]) m = axis_gap(c[j] - s, to[j], oo[j], h);
+        if (c[j] + s <= b1[j]) m = fminf(m, axis_gap(c[j] + s, to[j], oo[j], h));
+        if (m < FLT_MAX) lb2 = fminf(lb2, fmaf(m, m, gc[(j + 1) % 3] + gc[(j + 2) % 3]));
+      }
+      if (lb2 > bound) break;
+    }
+    const int xl = c[0] - s, xr = c[0] + s;
+    const bool has_l = xl >= b0[0], has_r = s > 0 && xr <= b1[0];
+    const float gxl = has_l ? axis_gap(xl, q.tx, g.ox, h) : 0.0f;
+    const float gxr = has_r ? axis_gap(xr, q.tx, g.ox, h) : 0.0f;
+    const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
+    const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
+    for (int kz = z0; kz <= z1; ++kz) {
+      const float gz = axis_gap(kz, q.tz, g.oz, h);
+      const float gz2 = gz * gz;
+      const bool zshell = kz == c[2] - s || kz == c[2] + s;
+      for (int jy = y0; jy <= y1; ++jy) {
+        const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
+        const float gy = axis_gap(jy, q.ty, g.oy, h);
+        const float gyz = fmaf(gy, gy, gz2);
+        if (gyz + gc[0] > bound) continue;
+        const int rowbase = (kz * g.dy + jy) * g.dx;
+        if (zshell || jy == c[1] - s || jy == c[1] + s) {
+          // a row on the ring's y/z faces: its x-range within the bound
+          int x0 = max(xl, b0[0]), x1 = min(xr, b1[0]);
+          if (bound < FLT_MAX) {
+            const float rem = fmaxf(bound - gyz, 0.0f);
+            const float rx = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
+            x0 = max(x0, cell_coord(q.tx - rx, g.ox, g.inv_h, g.dx));
+            x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
+          }
+          if (x0 <= x1)
+            lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + x0), __ldg(S.cell_start + rowbase + x1 + 1), band,
+                             best, second, bpos, borig, bD);
+        } else {
+          // a row inside the ring's y-z square: only its two end cells are on the ring
+          if (has_l && fmaf(gxl, gxl, gyz) <= bound)
+            lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + xl), __ldg(S.cell_start + rowbase + xl + 1), band,
+                             best, second, bpos, borig, bD);
+          if (has_r && fmaf(gxr, gxr, gyz) <= (EXACT ? bound : best * (1.0f + kRelPrune)))
+            lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + xr), __ldg(S.cell_start + rowbase + xr + 1), band,
+                             best, second, bpos, borig, bD);
+        }
+      }
+    }
+  }
+}
+
+// Nearest point strictly inside box q, searched by this lane alone: sorted
+// position and original index, or -1 when the box holds no point.
+__device__ __forceinline__ void lane_search(const SnapDev& S, const BoxQ& q, int& pos, int& orig) {
+  const GridParams& g = S.g;
+  pos = -1;
+  orig = -1;
+  if (!(q.lox < g.maxx && q.hix > g.minx && q.loy < g.maxy && q.hiy > g.miny && q.loz < g.maxz &&
+        q.hiz > g.minz && q.lox < q.hix && q.loy < q.hiy && q.loz < q.hiz))
+    return;
+  const int b0[3] = {cell_coord(q.lox, g.ox, g.inv_h, g.dx), cell_coord(q.loy, g.oy, g.inv_h, g.dy),
+                     cell_coord(q.loz, g.oz, g.inv_h, g.dz)};
+  const int b1[3] = {cell_coord(q.hix, g.ox, g.inv_h, g.dx), cell_coord(q.hiy, g.oy, g.inv_h, g.dy),
+                     cell_coord(q.hiz, g.oz, g.inv_h, g.dz)};
+  const int c[3] = {cell_coord(q.tx, g.ox, g.inv_h, g.dx), cell_coord(q.ty, g.oy, g.inv_h, g.dy),
+                    cell_coord(q.tz, g.oz, g.inv_h, g.dz)};
+  const float gx = axis_gap(c[0], q.tx, g.ox, g.h), gy = axis_gap(c[1], q.ty, g.oy, g.h),
+              gz = axis_gap(c[2], q.tz, g.oz, g.h);
+  const float gc[3] = {gx * gx, gy * gy, gz * gz};
+  float best = FLT_MAX, second = FLT_MAX;
+  int bpos = -1, borig = -1;
+  double bD = DBL_MAX;
+  lane_rings<false>(S, q, b0, b1, c, gc, 0.0f, best, second, bpos, borig, bD);
+  if (bpos < 0) return;
+  if (second <= best * (1.0f + kRelTie)) {
+    // possible FP64 tie (or an exact FP32 tie): re-rank the contenders
+    float fb = FLT_MAX, fs = FLT_MAX;
+    int p2 = -1, o2 = 0x7fffffff;
+    double D2 = DBL_MAX;
+    lane_rings<true>(S, q, b0, b1, c, gc, best * (1.0f + kRelTie), fb, fs, p2, o2, D2);
+    bpos = p2;
+    borig = o2;
+  }
+  pos = bpos;
+  orig = borig;
+}
+
+// Bit index of the n-th (from 0) set bit of lo | hi << 32.
+__device__ __forceinline__ int nth_set_bit(unsigned lo, unsigned hi, int n) {
+  const int nlo = __popc(lo);
+  if (n < nlo) return (int)__fns(lo, 0, n + 1);
+  return 32 + (int)__fns(hi, 0, n - nlo + 1);
+}
+
+__global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride, int kind) {
-  __shared__ SegSmem segs[kWarps];
-  __shared__ int fpos[kWarps][kSeg];    // the record's deferred samples: neighbour (sorted position)
-  __shared__ float fvlos[kWarps][kSeg]; // and its LOS speed
+  __shared__ int spos[kWarps][kDefBatch];    // neighbour (sorted position) of each staged sample
+  __shared__ float svlos[kWarps][kDefBatch]; // and its LOS speed (spectral)
   const int w = threadIdx.x >> 5;
-  SegSmem& sm = segs[w];
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
   const int64_t nrec = min((int64_t)a.counter[kCtrDeferred], a.deferred_cap);  // written by the march
   for (;;) {
-    unsigned long long idx = 0;
-    if (lane == 0) idx = atomicAdd(a.counter + kCtrDeferredHead, 1ull);
-    idx = __shfl_sync(kFull, idx, 0);
-    if ((int64_t)idx >= nrec) return;
-    const DeferredRec rec = a.deferred[idx];
-    RayCtx r;
-    if (!ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, r)) continue;  // records come from real rays only
-    const int s0 = (int)rec.y;
-    const unsigned f0 = rec.z, f1 = rec.w;
-    int pos[2] = {-1, -1}, orig[2] = {-1, -1};
-    resolve_deferred(a.snap, r, s0, f0, f1, sm, pos, orig, a.stats);
-    const ViewDesc* V = a.views + r.v;
-    const int nz = V->nz, nx = V->nx;
-    const int64_t ray = (int64_t)r.i * nx + r.j;
-    const bool need0 = (f0 >> lane) & 1u, need1 = (f1 >> lane) & 1u;
-    int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
-    if (nnout) {
-      if (need0) nnout[ray * nz + s0 + lane] = orig[0];
-      if (need1) nnout[ray * nz + s0 + 32 + lane] = orig[1];
-    }
-    const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
-    if (kind == kDeferredSpectral) {
-      // the deferred samples as a compact list, then lane = lambda bin as in
-      // the march (each sample is its own run)
-      const int n0 = __popc(f0), nf = n0 + __popc(f1);
-      const float ux = V->ux, uy = V->uy, uz = V->uz;
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        if (i ? need1 : need0) {
-          const int slot = i ? n0 + __popc(f1 & lt) : __popc(f0 & lt);
-          const int p = i ? pos[1] : pos[0];
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(a.counter + kCtrDeferredHead, 32ull);
+    base = __shfl_sync(kFull, base, 0);
+    if ((int64_t)base >= nrec) return;
+    const int64_t ri = (int64_t)base + lane;
+    DeferredRec rec = make_uint4(0u, 0u, 0u, 0u);
+    if (ri < nrec) rec = a.deferred[ri];
+    const int cnt = __popc(rec.z) + __popc(rec.w);
+    const int incl = warp_incl_scan(cnt);
+    const int excl = incl - cnt;
+    const int total = __shfl_sync(kFull, incl, 31);  // every lane takes part in the shuffle
+    if (a.stats && lane == 0) atomicAdd(a.stats + kStatFbUnion, (unsigned long long)total);
+    for (int r0 = 0; r0 < 32;) {
+      // records r0 .. r1-1 whose samples fit the staging arrays (a record has <= 64)
+      const int start = __shfl_sync(kFull, excl, r0);
+      const unsigned fits = __ballot_sync(kFull, lane >= r0 && incl - start <= kDefBatch);
+      const int r1 = r0 + max(__popc(fits), 1);
+      const int nsamp = __shfl_sync(kFull, incl, r1 - 1) - start;
+      // 1. one sample per lane: its record, ray and box, then its own search
+      for (int t0 = 0; t0 < nsamp; t0 += 32) {
+        const int t = t0 + lane;
+        const int own = warp_owner(incl, start + t);  // the record lane holding flattened sample t
+        const unsigned ox = __shfl_sync(kFull, rec.x, own & 31), oy = __shfl_sync(kFull, rec.y, own & 31);
+        const unsigned oz = __shfl_sync(kFull, rec.z, own & 31), ow = __shfl_sync(kFull, rec.w, own & 31);
+        const int oe = __shfl_sync(kFull, excl, own & 31);
+        if (t < nsamp) {
+          RayCtx r;
+          ray_of_item(a, ktab, ktab_stride, (int64_t)ox, r);  // records come from real rays only
+          const int k = (int)oy + nth_set_bit(oz, ow, start + t - oe);
+          int p, o;
+          lane_search(a.snap, exact_box(r, k), p, o);
+          const ViewDesc* V = a.views + r.v;
+          int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+          if (nnout) nnout[((int64_t)r.i * V->nx + r.j) * V->nz + k] = o;
           float vl = 0.0f;
-          if (p >= 0) {
+          if (p >= 0 && kind == kDeferredSpectral) {
             const float4 vv = __ldg(a.snap.vel + p);
-            vl = fmaf(uz, vv.z, fmaf(uy, vv.y, ux * vv.x));
+            vl = fmaf(V->uz, vv.z, fmaf(V->uy, vv.y, V->ux * vv.x));
           }
-          fpos[w][slot] = p;
-          fvlos[w][slot] = vl;
+          spos[w][t] = p;
+          svlos[w][t] = vl;
         }
       }
       __syncwarp();
-      const int L = V->L;
-      for (int l = 0; l < a.nlines; ++l) {
-        const LineDesc& D = LD[l];
-        if (!D.ew) continue;  // views may have fewer lines than the launch
-        const double scale = D.is_dn ? V->scale_dn : V->scale;
-        for (int m = 0; m < D.nw; ++m) {
-          const int il = D.wstart + 32 * m + lane;
-          const float lamv = il < L ? __ldg(D.lam + il) : 3.0e30f;
-          float part = 0.0f;
-          for (int f = 0; f < nf; ++f) {
-            const int p = fpos[w][f];
-            if (p < 0) continue;
-            const float2 pw = __ldg(D.ew + p);
-            if (pw.x == 0.0f) continue;  // intpolpeak ? ... : 0 (nn:204)
-            const float sc = __fdividef(2.0f, pw.y);
-            const float ns = -(fvlos[w][f] * D.shift_k) * sc;
-            const float q = fmaf(lamv, sc, ns);
-            part = fmaf(pw.x, ex2_approx(-q * q), part);
+      // 2. their emission, record by record
+      for (int rr = r0; rr < r1; ++rr) {
+        const int sn = __shfl_sync(kFull, cnt, rr);
+        const int so = __shfl_sync(kFull, excl, rr) - start;
+        const unsigned item = __shfl_sync(kFull, rec.x, rr);
+        if (sn == 0) continue;
+        RayCtx r;
+        ray_of_item(a, ktab, ktab_stride, (int64_t)item, r);
+        const ViewDesc* V = a.views + r.v;
+        const int64_t ray = (int64_t)r.i * V->nx + r.j;
+        const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
+        if (kind == kDeferredSpectral) {
+          const int L = V->L;
+          for (int l = 0; l < a.nlines; ++l) {
+            const LineDesc& D = LD[l];
+            if (!D.ew) continue;  // views may have fewer lines than the launch
+            const double scale = D.is_dn ? V->scale_dn : V->scale;
+            for (int m = 0; m < D.nw; ++m) {
+              const int il = D.wstart + 32 * m + lane;
+              const float lamv = il < L ? __ldg(D.lam + il) : 3.0e30f;
+              float part = 0.0f;
+              for (int f = so; f < so + sn; ++f) {
+                const int p = spos[w][f];
+                if (p < 0) continue;
+                const float2 pw = __ldg(D.ew + p);
+                if (pw.x == 0.0f) continue;  // intpolpeak ? ... : 0 (nn:204)
+                const float sc = __fdividef(2.0f, pw.y);
+                const float ns = -(svlos[w][f] * D.shift_k) * sc;
+                const float q = fmaf(lamv, sc, ns);
+                part = fmaf(pw.x, ex2_approx(-q * q), part);
+              }
+              if (il < L && part != 0.0f)
+                atomicAdd(D.out + ray * L + il, __double2float_rn(__dmul_rn(scale, (double)part)));
+            }
           }
-          if (il < L && part != 0.0f) atomicAdd(D.out + ray * L + il, __double2float_rn(__dmul_rn(scale, (double)part)));
+        } else {
+          const float* s2v = kind == kDeferredThomson ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
+          for (int l = 0; l < a.nlines; ++l) {
+            const LineDesc& D = LD[l];
+            if (!D.out) continue;
+            float val = 0.0f;
+            for (int f = so + lane; f < so + sn; f += 32) {
+              const int p = spos[w][f];
+              if (p >= 0) val += s2v ? fmaxf(__ldg(a.totpol + p).y * __ldg(s2v + p), 0.0f) : __ldg(D.ew + p).x;
+            }
+            const float sum = warp_sum(val);
+            if (lane == 0 && sum != 0.0f)
+              atomicAdd(D.out + ray, __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
+          }
         }
       }
-      __syncwarp();  // fpos/fvlos are rewritten by the next record
-    } else {
-      const float* s2v = kind == kDeferredThomson ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
-      for (int l = 0; l < a.nlines; ++l) {
-        const LineDesc& D = LD[l];
-        if (!D.out) continue;
-        float val = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 2; ++i) {
-          const int p = i ? pos[1] : pos[0];
-          if ((i ? need1 : need0) && p >= 0)
-            val += s2v ? fmaxf(__ldg(a.totpol + p).y * __ldg(s2v + p), 0.0f) : __ldg(D.ew + p).x;
-        }
-        const float sum = warp_sum(val);
-        if (lane == 0 && sum != 0.0f)
-          atomicAdd(D.out + ray, __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
-      }
+      __syncwarp();  // the staging arrays are rewritten by the next batch
+      r0 = r1;
     }
   }
 }
