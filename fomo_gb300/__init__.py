@@ -22,6 +22,7 @@ EINVAL, ENOMEM, EADMISSION, EDEVICE, ETIMEOUT, ENOTFOUND, EIO, ETABLE, ECANCELLE
     -1, -2, -3, -4, -5, -6, -7, -8, -9, -10, -11
 METHOD_NN = 0
 METHOD_THOMSON = 1
+METHOD_PROJECTION = 2
 OBS_SPECTROSCOPIC = 1
 OBS_IMAGING = 2
 SPEED_OF_LIGHT = 2.99792458e8

@@ -31,7 +31,7 @@ struct SnapDev {
 // One view (l, b) of one snapshot.  Host fills the first block (trig values
 // come from the host libm, as in the reference); the device fills the rest.
 // ---------------------------------------------------------------------------
-enum Method : int { kMethodNN = 0, kMethodThomson = 1 };
+enum Method : int { kMethodNN = 0, kMethodThomson = 1, kMethodProjection = 2 };
 
 struct ViewDesc {
   // ---- host-filled
@@ -162,6 +162,10 @@ cudaError_t launch_speed_max(const float4* vel, int64_t n, unsigned int* vmax_bi
 cudaError_t launch_view_init(ViewDesc* views, int nviews, cudaStream_t s);
 cudaError_t launch_view_extents(SnapDev snap, ViewDesc* views, int nviews, float* s2, cudaStream_t s);
 cudaError_t launch_view_finalize(ViewDesc* views, int nviews, double3* ktab, int ktab_stride, cudaStream_t s);
+
+// projection.cu: the projection render of every view of a group (outputs zeroed beforehand)
+cudaError_t launch_projection(SnapDev snap, const ViewDesc* views, const LineDesc* lines, int nviews, int nlines,
+                              bool imaging, int sm_count, cudaStream_t s);
 
 // march.cu
 // The march: the first search pass and the emission sums of every ray, then

@@ -278,14 +278,15 @@ FoMoObservationType RenderCube::readobservationtype() { return observationtype; 
 
 namespace {
 
-enum class Method { kNN, kThomson };
+enum class Method { kNN, kThomson, kProjection };
 
 // The render methods of this library; the reference's CPU names select the
 // GPU renderers too.  Others raise, as the reference exits (fomo-object.cpp:430-434).
 Method method_of(const std::string& m) {
   if (m == "NearestNeighbour" || m == "NearestNeighbourGPU") return Method::kNN;
   if (m == "Thomson" || m == "ThomsonGPU") return Method::kThomson;
-  if (m == "CGAL" || m == "CGAL2D" || m == "Projection")
+  if (m == "Projection") return Method::kProjection;
+  if (m == "CGAL" || m == "CGAL2D")
     throw std::runtime_error("FoMo: render method " + m + " is not available in this library");
   throw std::runtime_error("Error: unknown rendering method.");
 }
@@ -563,7 +564,8 @@ void FoMoObject::render(const std::vector<double> lvec, const std::vector<double
       fomo_request& q = reqs[k];
       q.snapshot = D.snap;
       q.table = thomson ? 0 : table;
-      q.method = thomson ? FOMO_METHOD_THOMSON : FOMO_METHOD_NN;
+      q.method = thomson ? FOMO_METHOD_THOMSON
+                         : (method == Method::kProjection ? FOMO_METHOD_PROJECTION : FOMO_METHOD_NN);
       q.nx = nx;
       q.ny = ny;
       q.nz = nz;

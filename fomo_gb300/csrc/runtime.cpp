@@ -464,8 +464,11 @@ int get_thomson_payload(fomo_ctx* ctx, SnapRec& r, const float2** out) {
 
 // ---------------------------------------------------------------- rendering
 
+// Methods whose emission comes from a G(T, n) table (all but Thomson).
+bool uses_table(int method) { return method != FOMO_METHOD_THOMSON; }
+
 int validate(fomo_ctx* ctx, const fomo_request& q) {
-  if (q.method != FOMO_METHOD_NN && q.method != FOMO_METHOD_THOMSON)
+  if (q.method != FOMO_METHOD_NN && q.method != FOMO_METHOD_THOMSON && q.method != FOMO_METHOD_PROJECTION)
     return set_err(ctx, FOMO_EMETHOD, "Error: unknown rendering method.");
   if (q.nx < 2 || q.ny < 2 || q.nz < 1 || q.nlambda < 1)
     return set_err(ctx, FOMO_EINVAL, "resolution must have nx >= 2, ny >= 2, nz >= 1, nlambda >= 1");
@@ -473,7 +476,7 @@ int validate(fomo_ctx* ctx, const fomo_request& q) {
     return set_err(ctx, FOMO_EINVAL, "resolution too large (nx*ny < 2^30, nz <= 2^20, nlambda <= 256)");
   if (!std::isfinite(q.l) || !std::isfinite(q.b)) return set_err(ctx, FOMO_EINVAL, "view angles must be finite");
   if (ctx->snaps.find(q.snapshot) == ctx->snaps.end()) return set_err(ctx, FOMO_ENOTFOUND, "unknown snapshot id");
-  if (q.method == FOMO_METHOD_NN) {
+  if (uses_table(q.method)) {
     if (ctx->tables.find(q.table) == ctx->tables.end()) return set_err(ctx, FOMO_ENOTFOUND, "unknown table id");
     if (!(q.lambda_width > 0) && q.nlambda > 1)
       return set_err(ctx, FOMO_EINVAL, "lambda_width must be > 0 (m/s) for spectroscopic renders");
@@ -513,7 +516,8 @@ void fill_view_host(const fomo_request& q, double lambda0, int tw, int th, ViewD
   V->ny = q.ny;
   V->nz = q.nz;
   V->L = q.method == FOMO_METHOD_THOMSON ? 1 : q.nlambda;
-  V->method = q.method == FOMO_METHOD_THOMSON ? kMethodThomson : kMethodNN;
+  V->method = q.method == FOMO_METHOD_THOMSON ? kMethodThomson
+              : (q.method == FOMO_METHOD_PROJECTION ? kMethodProjection : kMethodNN);
   V->ray_tile_w = tw;
   V->ray_tile_h = th;
 }
@@ -528,7 +532,7 @@ void view_info_from(const ViewDesc& V, const fomo_request& q, const TableHost* t
   info->maxdistance = V.md;
   info->deltaz = V.deltaz;
   info->pathlength = V.pathlength;
-  const bool dn = t && t->is_dn && q.method == FOMO_METHOD_NN;
+  const bool dn = t && t->is_dn && uses_table(q.method);
   info->apix = dn ? V.apix : 1.0;
   info->scale = dn ? V.scale_dn : V.scale;
   info->lambda0 = q.method == FOMO_METHOD_THOMSON ? 0.0 : (t ? t->lambda0 : 0.0);
@@ -566,7 +570,9 @@ std::string workload_class(const PlanGroup& G, const SnapRec& snap) {
   std::ostringstream k;
   int lg = 0;
   for (int64_t n = snap.n; n > 1; n >>= 1) ++lg;
-  k << (G.method == FOMO_METHOD_THOMSON ? "thomson" : (G.imaging ? "imaging" : "spectral")) << ":nl" << G.nl << ":L"
+  k << (G.method == FOMO_METHOD_THOMSON ? "thomson"
+        : (G.method == FOMO_METHOD_PROJECTION ? (G.imaging ? "proj-imaging" : "proj-spectral")
+                                              : (G.imaging ? "imaging" : "spectral"))) << ":nl" << G.nl << ":L"
     << G.maxL << ":nz" << G.maxnz << ":n2^" << lg;
   return k.str();
 }
@@ -709,7 +715,7 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     G.any_nn = false;
     for (int v = 0; v < G.nv; ++v) {
       const fomo_request& q0 = reqs[G.vreqs[v][0]];
-      const TableHost* t0 = q0.method == FOMO_METHOD_NN ? &ctx->tables[q0.table].h : nullptr;
+      const TableHost* t0 = uses_table(q0.method) ? &ctx->tables[q0.table].h : nullptr;
       fill_view_host(q0, t0 ? t0->lambda0 : 0.0, G.tw, G.th, &hv[v]);
       hv[v].xt = dxy + (size_t)v * (G.maxnx + G.maxny);
       hv[v].yt = hv[v].xt + G.maxnx;
@@ -721,7 +727,7 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
         const fomo_request& q = reqs[r];
         LineDesc& LD = hl[(size_t)v * G.nl + li];
         LD.out = d_out[r];
-        if (q.method == FOMO_METHOD_NN) {
+        if (uses_table(q.method)) {
           const TableHost& t = ctx->tables[q.table].h;
           LD.ew = G.ew[r];
           LD.lambda0 = t.lambda0;
@@ -741,6 +747,12 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
           LD.is_dn = 0;
         }
         plan->view_of_req[r] = vbase + v;
+        if (q.method == FOMO_METHOD_PROJECTION) {
+          // the projection accumulates into the output with atomics: zeroed first
+          G.zero_outs.push_back({d_out[r], sizeof(float) * cube_elems(q)});
+          if (d_nn && d_nn[r])
+            return set_err(ctx, FOMO_EINVAL, "a projection render has no per-sample neighbour indices");
+        }
         if (d_nn && d_nn[r]) {
           hnn[v] = d_nn[r];
           G.any_nn = true;
@@ -803,9 +815,14 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s)
     a.totpol = G.totpol;
     a.stats = ctx->march_stats;
     if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = record_timing(scr->ev0);
-    if (e == cudaSuccess)
+    if (G.method == FOMO_METHOD_PROJECTION) {
+      for (const auto& z : G.zero_outs)
+        if (e == cudaSuccess) e = cudaMemsetAsync(z.first, 0, z.second, s);
+      if (e == cudaSuccess) e = launch_projection(sd, dv, a.lines, G.nv, G.nl, G.imaging, ctx->sm_count, s);
+    } else if (e == cudaSuccess) {
       e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
                        G.method == FOMO_METHOD_THOMSON || G.imaging);
+    }
     if (e == cudaSuccess && scr->ev1 && ctx->time_march) e = record_timing(scr->ev1);
   }
   if (e != cudaSuccess) return cuda_err(ctx, e, "render launch");
@@ -1107,7 +1124,7 @@ int fomo_render_device(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube
     FOMO_CUDA(cudaStreamSynchronize(s), "render");
     rc = finish_views(ctx, &views);
     if (rc) return rc;
-    const TableHost* t = req->method == FOMO_METHOD_NN ? &ctx->tables[req->table].h : nullptr;
+    const TableHost* t = uses_table(req->method) ? &ctx->tables[req->table].h : nullptr;
     view_info_from(views[vof[0]], *req, t, info);
   }
   return FOMO_OK;
@@ -1145,7 +1162,7 @@ int fomo_render_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* 
     rc = finish_views(ctx, &views);
     if (rc) return rc;
     for (int r = 0; r < nreq; ++r) {
-      const TableHost* t = reqs[r].method == FOMO_METHOD_NN ? &ctx->tables[reqs[r].table].h : nullptr;
+      const TableHost* t = uses_table(reqs[r].method) ? &ctx->tables[reqs[r].table].h : nullptr;
       view_info_from(views[vof[r]], reqs[r], t, &infos[r]);
     }
   }
@@ -1178,7 +1195,7 @@ int fomo_render(fomo_ctx* ctx, const fomo_request* req, float* out_cube, int32_t
   if (info) {
     rc = finish_views(ctx, &views);
     if (rc) return rc;
-    const TableHost* t = req->method == FOMO_METHOD_NN ? &ctx->tables[req->table].h : nullptr;
+    const TableHost* t = uses_table(req->method) ? &ctx->tables[req->table].h : nullptr;
     view_info_from(views[vof[0]], *req, t, info);
   }
   return FOMO_OK;

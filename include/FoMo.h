@@ -11,13 +11,14 @@
 //   * FoMoObject::render runs on the GPU through the C ABI of fomo_gpu.h.  The
 //     method names "NearestNeighbour" and "NearestNeighbourGPU" select the
 //     nearest-neighbour renderer, "Thomson" and "ThomsonGPU" the Thomson pB
-//     renderer.  The emissivity (or Thomson terms) is computed on the device
+//     renderer, "Projection" the projection renderer (each point added to the
+//     pixel nearest its projection).  The emissivity (or Thomson terms) is computed on the device
 //     from the DataCube and kept resident with the snapshot while the data do
 //     not change; several (l, b) views render in one batched launch.
 //   * Errors throw std::runtime_error (the reference prints and exits): an
 //     unknown or unavailable method, a missing or malformed table, a failed
 //     imaging-table check, no usable CUDA device.
-//   * "CGAL", "CGAL2D" and "Projection" are not part of this library.
+//   * "CGAL" and "CGAL2D" are not part of this library.
 //   * Gzipped output (setwriteoutzip) is a valid .gz stream written with
 //     stored deflate blocks; its uncompressed content is byte-identical.
 //

@@ -50,6 +50,8 @@ extern "C" {
 
 #define FOMO_METHOD_NN 0       /* "NearestNeighbourGPU" */
 #define FOMO_METHOD_THOMSON 1  /* "ThomsonGPU" */
+#define FOMO_METHOD_PROJECTION 2 /* "Projection": each point added to the pixel nearest its projection
+                                    (fomo-projection.cpp:17-193); no LOS march, nz only sets the path length */
 
 #define FOMO_OBS_SPECTROSCOPIC 1 /* FoMo::Spectroscopic (FoMo.h:120-125) */
 #define FOMO_OBS_IMAGING 2       /* FoMo::Imaging */
@@ -128,7 +130,7 @@ int fomo_thomson_emission(fomo_ctx* ctx, int snapshot, float* tot, float* pol);
 typedef struct {
   int snapshot;          /* fomo_snapshot_create id */
   int table;             /* fomo_table_* id (ignored for Thomson) */
-  int method;            /* FOMO_METHOD_NN or FOMO_METHOD_THOMSON */
+  int method;            /* FOMO_METHOD_NN, FOMO_METHOD_THOMSON or FOMO_METHOD_PROJECTION */
   int nx, ny, nz;        /* x_pixel, y_pixel, z_pixel (nx, ny >= 2) */
   int nlambda;           /* lambda_pixel: 1 = imaging, > 1 = spectroscopic (fomo-object.cpp:381-384) */
   double l, b;           /* view angles in radians */

@@ -173,6 +173,23 @@ def thomson_render(snap, tot, pol, l, b, nx, ny, nz, mode=0, nthreads=0, rows=No
     return cube, idx, view
 
 
+def projection_render(snap, eps, w, lambda0, l, b, nx, ny, nz, L, lambda_width, is_dn=False, mode=0,
+                      want_pix=False):
+    """Projection render (fomo-projection.cpp:17-193); returns (cube[ny, nx, L] float64,
+    pixel index per point or None, view record)."""
+    cube = np.zeros(nx * ny * L, np.float64)
+    pix = np.zeros(snap.npoints, np.int32) if want_pix else None
+    view = np.zeros(V_COUNT)
+    rc = lib().fo_projection_render(ctypes.c_long(snap.npoints), _fp(snap.x), _fp(snap.y), _fp(snap.z),
+                                    _fp(_c32(eps)), _fp(_c32(w)), _fp(snap.vx), _fp(snap.vy), _fp(snap.vz),
+                                    ctypes.c_double(lambda0), ctypes.c_double(l), ctypes.c_double(b), nx, ny, nz, L,
+                                    ctypes.c_double(lambda_width), int(is_dn), int(mode), _dp(cube), _ip(pix),
+                                    _dp(view))
+    if rc != 0:
+        raise RuntimeError(f"fo_projection_render failed: {rc}")
+    return cube.reshape(ny, nx, L), pix, view
+
+
 def render_grid(nx, ny, L, view, lambda0, is_dn=False):
     n = nx * ny * L
     gx = np.zeros(n, np.float32)

@@ -737,3 +737,82 @@ void fo_render_grid(int nx, int ny, int L, const double* view, double lambda0, i
     }
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* f2: projection render (fomo-projection.cpp:17-193)                       */
+/* ------------------------------------------------------------------------ */
+
+int fo_projection_render(long n, const float* x, const float* y, const float* z, const float* peak,
+                         const float* fwhm, const float* vx, const float* vy, const float* vz, double lambda0,
+                         double l, double b, int nx, int ny, int nz, int L, double lambda_width, int is_dn, int mode,
+                         double* cube, int32_t* pix, double* view) {
+  if (n <= 0 || nx < 2 || ny < 2 || nz < 1 || L < 1) return FO_EARG;
+  const double cb = cos(b), sb = sin(b), cl = cos(l), sl = sin(l);
+  double* losvel = (double*)malloc(sizeof(double) * (size_t)n);
+  float* accf = (float*)calloc((size_t)nx * ny * L, sizeof(float));
+  if (!losvel || !accf) {
+    free(losvel);
+    free(accf);
+    return FO_EARG;
+  }
+  double ext[6];
+  nn_extents(n, x, y, z, vx, vy, vz, cb, sb, cl, sl, ext, losvel); /* :37-61 */
+  const double minx = ext[0], maxx = ext[1], miny = ext[2], maxy = ext[3], minz = ext[4], maxz = ext[5];
+  const double lambda_width_in_A = lambda_width * lambda0 / FO_SPEED_OF_LIGHT; /* :65 */
+  const double c = FO_SPEED_OF_LIGHT;
+  const long total = (long)nx * ny * L;
+  for (long e = 0; e < total; ++e) cube[e] = 0.0;
+  /* the points in order, as the reference's loop runs on one thread (:121-159) */
+  for (long k = 0; k < n; ++k) {
+    const double gx = x[k], gy = y[k], gz = z[k];
+    const double xa = gx * cb * cl - gy * cb * sl - gz * sb; /* :47 */
+    const double ya = gx * sl + gy * cl;                     /* :48 */
+    const int j = (int)round((xa - minx) * (nx - 1) / (maxx - minx)); /* :124 */
+    const int i = (int)round((ya - miny) * (ny - 1) / (maxy - miny)); /* :126 */
+    if (pix) pix[k] = i * nx + j;
+    if (L > 1) {
+      for (int il = 0; il < L; ++il) {
+        const double lambdaval = (double)il / (L - 1) * lambda_width_in_A - lambda_width_in_A / 2.; /* :133 */
+        /* :134; GCC expands pow(x, 2) to x*x */
+        const double dl = lambdaval - losvel[k] / c * lambda0;
+        const double w = fwhm[k];
+        const double tempintens = (double)peak[k] * exp(-(dl * dl) / (w * w) * 4. * log(2.));
+        const long ind = ((long)i * nx + j) * L + il;
+        if (mode & 1)
+          accf[ind] = (float)((double)accf[ind] + tempintens);
+        else
+          cube[ind] += tempintens;
+      }
+    } else {
+      const long ind = (long)i * nx + j;
+      if (mode & 1)
+        accf[ind] = accf[ind] + peak[k]; /* float += float (:152) */
+      else
+        cube[ind] += peak[k];
+    }
+  }
+  /* scaling as the NN render (:161-191) */
+  double pathlength = (maxz - minz) / (nz - 1);
+  if ((maxz == minz) || (nz == 1)) pathlength = 1.;
+  double apix = 1.;
+  if (is_dn) {
+    float dx = (float)((maxx - minx) / (nx - 1)), dy = (float)((maxy - miny) / (ny - 1));
+    const double as = M_PI / 180. / 3600.;
+    apix = ((double)dx / FO_MM_PER_ARCSEC) * ((double)dy / FO_MM_PER_ARCSEC) * (as * as);
+  }
+  const double scale = pathlength * 1e8 * apix;
+  for (long e = 0; e < total; ++e)
+    cube[e] = (mode & 1) ? (double)(float)(scale * (double)accf[e]) : scale * cube[e];
+  if (view) {
+    for (int d = 0; d < 6; ++d) view[d] = ext[d];
+    view[FO_V_MAXDIST] = 0.0;
+    view[FO_V_DELTAZ] = 0.0;
+    view[FO_V_PATHLENGTH] = pathlength;
+    view[FO_V_APIX] = apix;
+    view[FO_V_SCALE] = scale;
+    view[FO_V_LAMBDA_WIDTH_A] = lambda_width_in_A;
+  }
+  free(accf);
+  free(losvel);
+  return FO_OK;
+}

@@ -88,6 +88,18 @@ int fo_thomson_render(long n, const float* x, const float* y, const float* z, co
                       double l, double b, int nx, int ny, int nz, int mode, int nthreads, int row0, int row1,
                       double* cube, int32_t* nnidx, double* view);
 
+/* Projection render (fomo-projection.cpp:17-193): every point adds its
+ * emission to the pixel nearest its projection, j = round((x' - minx)(nx-1) /
+ * (maxx - minx)), i likewise; spectroscopic points add their Gaussian to all L
+ * bins (no zero-peak guard, :145).  cube: ny*nx*L doubles.  pix (nullable): the
+ * pixel index i*nx + j of every point.  mode bit 0: accumulate in FP32 in point
+ * order as the reference does single-threaded.  view: FO_V_COUNT doubles
+ * (maxdistance unused, 0). */
+int fo_projection_render(long n, const float* x, const float* y, const float* z, const float* peak,
+                         const float* fwhm, const float* vx, const float* vy, const float* vz, double lambda0,
+                         double l, double b, int nx, int ny, int nz, int L, double lambda_width, int is_dn, int mode,
+                         double* cube, int32_t* pix, double* view);
+
 /* The per-element x, y (and lambda for L > 1) grids of the render cube
  * (fomo-nearestneighbour.cpp:152-153,209-211,254-260), from a view record. */
 void fo_render_grid(int nx, int ny, int L, const double* view, double lambda0, int is_dn, float* gx, float* gy,

@@ -11,6 +11,7 @@ synthetic cases and stores inputs and outputs as compressed .npz files:
     nn_edges.npz     ragged sizes, nz = 1, empty corners, out-of-table points
     thomson.npz      Thomson (pB) views
     nn_medium.npz    a larger spectroscopic case (24^3 points, 32x32x48, L = 32)
+    projection.npz   Projection renders (spectroscopic, and imaging with a DN table)
     writer_*.txt/.dat the reference's own text and binary output files of three
                      small renders (spectroscopic, DN imaging, Thomson), with
                      their inputs in writers.npz
@@ -30,6 +31,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
+# one OpenMP thread: the reference's projection renderer accumulates with
+# `omp atomic` in thread order; single-threaded its float sums are reproducible
+os.environ["OMP_NUM_THREADS"] = "1"
 
 import oracle  # noqa: E402
 from fomo_gb300 import synth  # noqa: E402
@@ -136,6 +140,14 @@ def main():
                         dst.write(src.read())
         finally:
             os.chdir(cwd)
+        # 7. projection renders (single-threaded reference: reproducible float sums)
+        d1 = _render_cases("Projection", s, t, [(0.3, 0.2), (1.1, -0.4)], 16, 12, 20, 16, 0.6, tmp)
+        d2 = _render_cases("Projection", s, bt, [(0.4, 0.3)], 15, 11, 20, 1, 1e5, tmp)
+        eps_b, w_b = oracle.ref_emission(s, bp, imaging=True)
+        eps_s, w_s = oracle.ref_emission(s, tp)
+        np.savez_compressed(os.path.join(HERE, "projection.npz"), eps=eps_s, fwhm=w_s, eps_band=eps_b,
+                            fwhm_band=w_b, **_snap_dict(s), **_table_dict(t), **_table_dict(bt, "band"),
+                            **{k + "_a": v for k, v in d1.items()}, **{k + "_b": v for k, v in d2.items()}, **info)
         np.savez_compressed(os.path.join(HERE, "writers.npz"), **{"nn_" + k: v for k, v in _snap_dict(ws).items()},
                             **{"th_" + k: v for k, v in _snap_dict(wt).items()}, **_table_dict(t),
                             **_table_dict(bt, "band"), **info)

@@ -102,6 +102,23 @@ def test_thomson_render_mirror_is_bit_exact():
         assert G.norm_max_err(fp64.ravel(), cubes[v]) <= 1e-5
 
 
+@pytest.mark.parametrize("suffix,ek,wk,tk", [("_a", "eps", "fwhm", "table_text"),
+                                              ("_b", "eps_band", "fwhm_band", "band_text")])
+def test_projection_render_mirror_is_bit_exact_and_fp64_close(suffix, ek, wk, tk):
+    d = G.load("projection.npz")
+    s = G.snapshot(d)
+    t = G.table(d, tk)
+    views, nx, ny, nz, L, cubes, metas = _nn_cases(d, suffix)
+    for v, (l, b) in enumerate(views):
+        mirror, pix, _ = oracle.projection_render(s, d[ek], d[wk], t.lambda0, l, b, nx, ny, nz, L, metas[v][4],
+                                                  is_dn=t.is_dn, mode=1, want_pix=True)
+        _check_bits(mirror.ravel(), cubes[v], d)
+        assert pix.min() >= 0 and pix.max() < nx * ny
+        fp64, _, _ = oracle.projection_render(s, d[ek], d[wk], t.lambda0, l, b, nx, ny, nz, L, metas[v][4],
+                                              is_dn=t.is_dn, mode=0)
+        assert G.norm_max_err(fp64.ravel(), cubes[v]) <= 1e-5
+
+
 @pytest.mark.parametrize("name", ["nn_spectro.npz", "nn_imaging.npz"])
 def test_render_grids_match_reference(name):
     d = G.load(name)
