@@ -83,6 +83,9 @@ SIGNATURES = {
     "fomo_host_unregister": [ctypes.c_void_p, ctypes.c_void_p],
     "fomo_snapshot_create": [ctypes.c_void_p, ctypes.c_int64] + [_F] * 8 + [ctypes.POINTER(ctypes.c_int)],
     "fomo_snapshot_destroy": [ctypes.c_void_p, ctypes.c_int],
+    "fomo_snapshot_create_device": [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 8 + [ctypes.POINTER(ctypes.c_int)],
+    "fomo_abundance_ratio": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                             ctypes.POINTER(ctypes.c_double)],
     "fomo_snapshot_get_info": [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SnapshotInfo)],
     "fomo_table_create": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_char_p,
                           ctypes.c_int, ctypes.c_int, _F, _F, _F, ctypes.POINTER(ctypes.c_int)],
@@ -183,6 +186,13 @@ class Context:
         sid = ctypes.c_int()
         self._check(self._L.fomo_snapshot_create(self.h, arrs[0].shape[0], *[_fp(a) for a in arrs],
                                                  ctypes.byref(sid)))
+        return sid.value
+
+    def snapshot_device(self, n: int, ptrs) -> int:
+        """Snapshot from 8 device arrays (x, y, z, n, T, vx, vy, vz; z may be 0)."""
+        sid = ctypes.c_int()
+        self._check(self._L.fomo_snapshot_create_device(self.h, n, *[ctypes.c_void_p(p) if p else None for p in ptrs],
+                                                        ctypes.byref(sid)))
         return sid.value
 
     def snapshot_info(self, sid: int) -> SnapshotInfo:
@@ -356,6 +366,16 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def abundance_ratio(abund_file: str, standard_file: str, ion: str) -> float:
+    """Abundance renormalisation of `ion`'s element: (X/H) in abund_file over (X/H)
+    in standard_file (fomo_abundance_ratio in the C ABI)."""
+    r = ctypes.c_double()
+    rc = lib().fomo_abundance_ratio(None, abund_file.encode(), standard_file.encode(), ion.encode(), ctypes.byref(r))
+    if rc != OK:
+        raise FomoError(rc, f"abundance files {abund_file!r} / {standard_file!r} do not give {ion!r}")
+    return r.value
 
 
 def render_grid(nx, ny, L, info: ViewInfo, is_dn: bool):

@@ -341,6 +341,7 @@ struct FoMoObject::Device {
   unsigned long long gen = ~0ull;
   int64_t npoints = 0;
   std::map<std::string, int> tables;  // loaded G(T) tables by path
+  double abundratio = 1.0;            // of the last render
   ~Device() {
     if (!ctx) return;
     if (snap >= 0) fomo_snapshot_destroy(ctx, snap);
@@ -438,7 +439,8 @@ GoftCube FoMoObject::readgoftcube() {
       auto it = device_->tables.find(goftcube.readchiantifile());
       if (it == device_->tables.end()) throw std::runtime_error("FoMo: table of the last render is not loaded");
       const bool imaging = rendering.readobservationtype() == Imaging;
-      check(ctx, fomo_emission(ctx, device_->snap, it->second, imaging ? 1 : 0, 1.0, a.data(), w.data()),
+      check(ctx, fomo_emission(ctx, device_->snap, it->second, imaging ? 1 : 0, device_->abundratio, a.data(),
+                               w.data()),
             "emission");
       char unit[256] = {0};
       check(ctx, fomo_table_get_info(ctx, it->second, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, unit,
@@ -524,15 +526,29 @@ void FoMoObject::render(const std::vector<double> lvec, const std::vector<double
     } else {
       table = it->second;
     }
-    // any abundance file but "/empty" fails in the reference (its built-in
-    // standard abundances are an empty string, fomo-CHIANTI.cpp:21,264-273)
+    // abundance renormalisation of spectroscopic renders (fomo-CHIANTI.cpp:
+    // 264-273) against the standard abundances the tables were made with.  The
+    // reference's built-in copy of those is an empty string at the point of use
+    // (fomo-CHIANTI.cpp:21), so any file but "/empty" fails there; here the
+    // standard file is FOMO_STANDARD_ABUND, and without it the same error.
     const std::string af = rendering.readabundfile();
-    if (!imaging && af != "/empty") throw std::runtime_error("Error: invalid CHIANTI abundance file");
+    if (!imaging && af != "/empty") {
+      const char* std_file = std::getenv("FOMO_STANDARD_ABUND");
+      if (!std_file || !*std_file)
+        throw std::runtime_error("Error: invalid CHIANTI abundance file (set FOMO_STANDARD_ABUND to the standard "
+                                 "abundance file the G(T) tables were computed with)");
+      char ion[64] = {0};
+      check(ctx, fomo_table_get_info(ctx, table, nullptr, nullptr, nullptr, nullptr, nullptr, ion, (int)sizeof(ion),
+                                     nullptr, 0),
+            "table info");
+      check(ctx, fomo_abundance_ratio(ctx, af.c_str(), std_file, ion, &abundratio), "abundance");
+    }
     goft.setchiantifile(tf);
     goft.setabundfile(af);
     goft.setlambda0(rendering.readlambda0());
   }
   goft.setwriteoptions(wopt);
+  D.abundratio = abundratio;
   goftcube = goft;
   goft_pending_ = true;
 

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -263,7 +264,8 @@ int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec
   for (int k = 0; k < 8; ++k) a[k] = stage + (size_t)k * n;
   for (int k = 0; k < 8; ++k) {
     if (host[k]) {
-      cudaError_t e = cudaMemcpyAsync(a[k], host[k], sizeof(float) * n, cudaMemcpyHostToDevice, s);
+      // host or device memory alike (unified addressing: a device array is copied on the device)
+      cudaError_t e = cudaMemcpyAsync(a[k], host[k], sizeof(float) * n, cudaMemcpyDefault, s);
       if (e != cudaSuccess) {
         dev_free(ctx, stage);
         return cuda_err(ctx, e, "snapshot upload");
@@ -466,6 +468,39 @@ int get_thomson_payload(fomo_ctx* ctx, SnapRec& r, const float2** out) {
 
 // Methods whose emission comes from a G(T, n) table (all but Thomson).
 bool uses_table(int method) { return method != FOMO_METHOD_THOMSON; }
+
+// Relative abundance 10^(A_element - A_H) of the element of `ion` ("fe_12" ->
+// "fe") in a CHIANTI abundance file: lines "Z  A  symbol" until a negative Z
+// (fomo-CHIANTI.cpp:23-62; the symbol compare is case-insensitive and whole).
+bool abundance_of(const char* path, const char* ion, double* out, std::string* err) {
+  std::ifstream in(path);
+  if (!in) {
+    *err = std::string("Error: no CHIANTI abundance file exists: ") + path;
+    return false;
+  }
+  std::string name(ion);
+  name = name.substr(0, name.find('_'));
+  auto same = [](const std::string& p, const std::string& q) {
+    if (p.size() != q.size()) return false;
+    for (size_t i = 0; i < p.size(); ++i)
+      if (std::tolower((unsigned char)p[i]) != std::tolower((unsigned char)q[i])) return false;
+    return true;
+  };
+  double h = 0, el = 0, value = 0;
+  int z = 0;
+  std::string sym;
+  while (in >> z && z >= 0) {
+    if (!(in >> value >> sym)) break;
+    if (same(sym, "h")) h = value;
+    if (same(sym, name)) el = value;
+  }
+  if (h == 0.0 || el == 0.0) {
+    *err = std::string("Error: invalid CHIANTI abundance file (no H or no ") + name + "): " + path;
+    return false;
+  }
+  *out = std::pow(10.0, el - h);
+  return true;
+}
 
 int validate(fomo_ctx* ctx, const fomo_request& q) {
   if (q.method != FOMO_METHOD_NN && q.method != FOMO_METHOD_THOMSON && q.method != FOMO_METHOD_PROJECTION)
@@ -994,6 +1029,33 @@ int fomo_snapshot_create(fomo_ctx* ctx, int64_t n, const float* x, const float* 
   int nid = ctx->next_id++;
   ctx->snaps[nid] = r;
   *id = nid;
+  return FOMO_OK;
+}
+
+int fomo_snapshot_create_device(fomo_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
+                                const float* n_e, const float* T, const float* vx, const float* vy, const float* vz,
+                                int* id) {
+  if (!ctx || !id) return FOMO_EINVAL;
+  const float* arrs[8] = {x, y, z, n_e, T, vx, vy, vz};
+  for (const float* p : arrs) {
+    if (!p) continue;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess || at.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      return set_err(ctx, FOMO_EINVAL, "fomo_snapshot_create_device needs device arrays");
+    }
+  }
+  return fomo_snapshot_create(ctx, n, x, y, z, n_e, T, vx, vy, vz, id);
+}
+
+int fomo_abundance_ratio(fomo_ctx* ctx, const char* abund_file, const char* standard_file, const char* ion,
+                         double* ratio) {
+  if (!abund_file || !standard_file || !ion || !ratio) return FOMO_EINVAL;
+  double a = 0, b = 0;
+  std::string err;
+  if (!abundance_of(abund_file, ion, &a, &err) || !abundance_of(standard_file, ion, &b, &err))
+    return ctx ? set_err(ctx, FOMO_ETABLE, err) : FOMO_ETABLE;
+  *ratio = a / b;
   return FOMO_OK;
 }
 

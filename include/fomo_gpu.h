@@ -87,6 +87,13 @@ int fomo_snapshot_create(fomo_ctx* ctx, int64_t n, const float* x, const float* 
                          const float* n_e, const float* T, const float* vx, const float* vy, const float* vz,
                          int* id);
 int fomo_snapshot_destroy(fomo_ctx* ctx, int id);
+/* The same from arrays already in this device's memory (e.g. a simulation
+ * running on the GPU): no host round trip.  The arrays are copied into the
+ * snapshot's own storage on the context's stream, so work that writes them must
+ * be complete before the call; they may be freed after it returns. */
+int fomo_snapshot_create_device(fomo_ctx* ctx, int64_t n, const float* x, const float* y, const float* z,
+                                const float* n_e, const float* T, const float* vx, const float* vy, const float* vz,
+                                int* id);
 
 typedef struct {
   int64_t npoints;
@@ -118,6 +125,17 @@ int fomo_table_get_info(fomo_ctx* ctx, int id, double* lambda0, double* atweight
  * FoMoObject::readgoftcube() exposes (fomo-object.cpp:71-74).  imaging selects
  * FoMo::Imaging.  Computed on the device (and cached for later renders). */
 int fomo_emission(fomo_ctx* ctx, int snapshot, int table, int imaging, double abundratio, float* eps, float* fwhm);
+
+/* Abundance renormalisation of a spectral line (fomo-CHIANTI.cpp:23-62,
+ * 264-273): the element abundance relative to hydrogen in `abund_file` over the
+ * same in `standard_file` (the abundances the G(T) tables were computed with,
+ * e.g. CHIANTI's sun_coronal_2012_schmelz.abund).  Pass the result as a
+ * request's abundratio.  The reference compares against a built-in copy of the
+ * standard file that is empty at the point of use (fomo-CHIANTI.cpp:21), so
+ * any file but "/empty" fails there; here the standard file is an argument.
+ * ion: the table's ion string ("fe_12": element "fe").  ctx may be NULL. */
+int fomo_abundance_ratio(fomo_ctx* ctx, const char* abund_file, const char* standard_file, const char* ion,
+                         double* ratio);
 
 /* Per-point Thomson scattering terms of a snapshot, in its original point
  * order: tot = n * total term, pol = n * polarised term, the GoftCube vars

@@ -257,3 +257,26 @@ def ref_render_and_write(method: str, snap, table_path: str, l, b, nx, ny, nz, L
                                     ctypes.c_double(lambda_width), int(options), out_path.encode())
     if rc != 0:
         raise RuntimeError(ref().ref_last_error().decode())
+
+
+def abundance_ratio(abund_file: str, standard_file: str, ion: str) -> float:
+    """Restatement of abundfromchianti (fomo-CHIANTI.cpp:23-62) applied to both
+    files and divided as at fomo-CHIANTI.cpp:264-273: 10^(A_el - A_H) of the
+    ion's element ("fe_12" -> "fe", case-insensitive whole-symbol match) in
+    abund_file over the same in standard_file."""
+    def rel(path):
+        name = ion.split("_")[0].lower()
+        h = el = 0.0
+        toks = open(path).read().split()
+        i = 0
+        while i + 2 < len(toks) + 0 and int(float(toks[i])) >= 0:
+            value, sym = float(toks[i + 1]), toks[i + 2].lower()
+            if sym == "h":
+                h = value
+            if sym == name:
+                el = value
+            i += 3
+        if h == 0.0 or el == 0.0:
+            raise ValueError(f"invalid abundance file {path}")
+        return 10.0 ** (el - h)
+    return rel(abund_file) / rel(standard_file)

@@ -146,3 +146,23 @@ def test_full_size_plain_config_sampled_rows(ctx):
             assert G.norm_max_err(cube[r0:r0 + 2].ravel(), oc.ravel()) <= 1e-4
     assert (idx >= 0).mean() > 0.5
     ctx.drop_snapshot(sid)
+
+
+def test_snapshot_from_device_arrays_renders_the_same(ctx):
+    import torch
+    s = synth.loop_snapshot(16, seed=12)
+    t = synth.line_table()
+    tid = ctx.table(t)
+    dev = [torch.from_numpy(a.copy()).cuda() for a in s.arrays()]
+    sid_h = ctx.snapshot(s)
+    torch.cuda.synchronize()  # the arrays must be complete: the snapshot copies them on the context's stream
+    sid_d = ctx.snapshot_device(s.npoints, [d.data_ptr() for d in dev])
+    del dev  # the snapshot keeps its own copy
+    width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+    a, ia, _ = ctx.render(ctx.request(sid_h, tid, fg.METHOD_NN, 20, 16, 32, 16, 0.4, -0.2, width), want_idx=True)
+    b, ib, _ = ctx.render(ctx.request(sid_d, tid, fg.METHOD_NN, 20, 16, 32, 16, 0.4, -0.2, width), want_idx=True)
+    np.testing.assert_array_equal(ia, ib)
+    np.testing.assert_array_equal(a, b)
+    with pytest.raises(fg.FomoError) as ei:  # host arrays are refused by the device entry point
+        ctx.snapshot_device(s.npoints, [a.ctypes.data for a in s.arrays()])
+    assert ei.value.code == fg.EINVAL
