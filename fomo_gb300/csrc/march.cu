@@ -876,6 +876,23 @@ __device__ __forceinline__ void lane_search(const SnapDev& S, const BoxQ& q, int
   orig = borig;
 }
 
+// Ray context of lane `src` (every lane takes part).
+__device__ __forceinline__ RayCtx shfl_ray(const RayCtx& r, int src) {
+  RayCtx o;
+  o.v = __shfl_sync(kFull, r.v, src);
+  o.i = __shfl_sync(kFull, r.i, src);
+  o.j = __shfl_sync(kFull, r.j, src);
+  o.item = __shfl_sync(kFull, r.item, src);
+  o.A0 = __shfl_sync(kFull, r.A0, src);
+  o.A1 = __shfl_sync(kFull, r.A1, src);
+  o.A2 = __shfl_sync(kFull, r.A2, src);
+  o.md = __shfl_sync(kFull, r.md, src);
+  o.mdf = __shfl_sync(kFull, r.mdf, src);
+  o.kt = reinterpret_cast<const double3*>(
+      __shfl_sync(kFull, (unsigned long long)reinterpret_cast<uintptr_t>(r.kt), src));
+  return o;
+}
+
 // Bit index of the n-th (from 0) set bit of lo | hi << 32.
 __device__ __forceinline__ int nth_set_bit(unsigned lo, unsigned hi, int n) {
   const int nlo = __popc(lo);
@@ -903,6 +920,9 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
     const int excl = incl - cnt;
     const int total = __shfl_sync(kFull, incl, 31);  // every lane takes part in the shuffle
     if (a.stats && lane == 0) atomicAdd(a.stats + kStatFbUnion, (unsigned long long)total);
+    // each lane decodes its own record's ray once (view, pixel, FP64 ray terms)
+    RayCtx mine{};
+    if (cnt > 0) ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, mine);  // records come from real rays only
     for (int r0 = 0; r0 < 32;) {
       // records r0 .. r1-1 whose samples fit the staging arrays (a record has <= 64)
       const int start = __shfl_sync(kFull, excl, r0);
@@ -912,13 +932,12 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
       // 1. one sample per lane: its record, ray and box, then its own search
       for (int t0 = 0; t0 < nsamp; t0 += 32) {
         const int t = t0 + lane;
-        const int own = warp_owner(incl, start + t);  // the record lane holding flattened sample t
-        const unsigned ox = __shfl_sync(kFull, rec.x, own & 31), oy = __shfl_sync(kFull, rec.y, own & 31);
-        const unsigned oz = __shfl_sync(kFull, rec.z, own & 31), ow = __shfl_sync(kFull, rec.w, own & 31);
-        const int oe = __shfl_sync(kFull, excl, own & 31);
+        const int own = warp_owner(incl, start + t) & 31;  // the record lane holding flattened sample t
+        const unsigned oy = __shfl_sync(kFull, rec.y, own);
+        const unsigned oz = __shfl_sync(kFull, rec.z, own), ow = __shfl_sync(kFull, rec.w, own);
+        const int oe = __shfl_sync(kFull, excl, own);
+        const RayCtx r = shfl_ray(mine, own);
         if (t < nsamp) {
-          RayCtx r;
-          ray_of_item(a, ktab, ktab_stride, (int64_t)ox, r);  // records come from real rays only
           const int k = (int)oy + nth_set_bit(oz, ow, start + t - oe);
           int p, o;
           lane_search(a.snap, exact_box(r, k), p, o);
@@ -939,10 +958,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
       for (int rr = r0; rr < r1; ++rr) {
         const int sn = __shfl_sync(kFull, cnt, rr);
         const int so = __shfl_sync(kFull, excl, rr) - start;
-        const unsigned item = __shfl_sync(kFull, rec.x, rr);
+        const RayCtx r = shfl_ray(mine, rr);
         if (sn == 0) continue;
-        RayCtx r;
-        ray_of_item(a, ktab, ktab_stride, (int64_t)item, r);
         const ViewDesc* V = a.views + r.v;
         const int64_t ray = (int64_t)r.i * V->nx + r.j;
         const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
