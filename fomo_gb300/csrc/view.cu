@@ -1,10 +1,12 @@
 // K3: per-view set-up, entirely on the device (no host round trip).
 //
 //  * view_extents_kernel: Stage A of the reference (fomo-c/src/fomo-nearest-
-//    neighbour.cpp:76-108): every point rotated in FP64 with the reference's
+//    neighbour.cpp:76-108): the points rotated in FP64 with the reference's
 //    operand order, min/max reduced through order-preserving 64-bit atomics
-//    (exact, order independent).  For Thomson the pole-blended rotation with
-//    clamped cos/sin and sin^2(chi) per point (fomo-thomson.cpp:139-199).
+//    (exact, order independent).  An FP32 rotation with a proven error bound
+//    screens the points first, so only those near a running extreme are
+//    rotated in FP64.  For Thomson every point takes the pole-blended rotation
+//    with clamped cos/sin and sin^2(chi) (fomo-thomson.cpp:139-199).
 //  * view_finalize_kernel: maxdistance (nn:138 / thomson:249-260), delta z,
 //    path length and DN pixel area (nn:235-267), and the per-LOS-sample FP64
 //    table z_k*sin(b)*cos(l), z_k*sin(b)*sin(l), z_k*cos(b) that the march
@@ -14,6 +16,7 @@
 // the host libm and passed in; everything here is +, -, *, /, sqrt in IEEE
 // FP64 with explicit round-to-nearest intrinsics (no FMA contraction).
 #include <cuda_runtime.h>
+#include <float.h>
 #include <stdint.h>
 
 #include "fomo_internal.h"
@@ -61,7 +64,55 @@ __global__ void view_extents_kernel(SnapDev snap, ViewDesc* views, float* s2) {
   float* s2v = s2 ? s2 + (int64_t)blockIdx.y * snap.n : nullptr;
   // LOS unit for sin^2 chi (thomson:194): clamped sin_b/cos_b with cos(l), sin(l)
   const double u0 = __dmul_rn(sb, cl), u1 = __dmul_rn(-sb, sl), u2 = cb;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < snap.n;
+  if (!thomson) {
+    // The FP64 extremes are those of the points whose FP32 rotation comes
+    // within 2E of this thread's running FP32 extreme: |x32 - x64| <= E for
+    // every point, E = 2^-20 (max|x| + max|y| + max|z|) (the FP32 sum of three
+    // products of a coordinate and two trigonometric factors errs by less than
+    // 8 * 2^-24 of that), so the point of the FP64 extreme always passes.  Only
+    // those points are rotated in FP64.
+    const GridParams& g = snap.g;
+    const float E = ldexpf(fmaxf(fabsf(g.minx), fabsf(g.maxx)) + fmaxf(fabsf(g.miny), fabsf(g.maxy)) +
+                               fmaxf(fabsf(g.minz), fabsf(g.maxz)),
+                           -20);
+    const float E2 = 2.0f * E;
+    const float cbf = (float)cb, sbf = (float)sb, clf = (float)cl, slf = (float)sl;
+    float rmn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, rmx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < snap.n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const float4 p = snap.pts[i];
+      const float x32 = (p.x * cbf) * clf - (p.y * cbf) * slf - p.z * sbf;
+      const float y32 = p.x * slf + p.y * clf;
+      const float z32 = (p.x * sbf) * clf - (p.y * sbf) * slf + p.z * cbf;
+      const bool near = x32 < rmn[0] + E2 || x32 > rmx[0] - E2 || y32 < rmn[1] + E2 || y32 > rmx[1] - E2 ||
+                        z32 < rmn[2] + E2 || z32 > rmx[2] - E2;
+      rmn[0] = fminf(rmn[0], x32);
+      rmx[0] = fmaxf(rmx[0], x32);
+      rmn[1] = fminf(rmn[1], y32);
+      rmx[1] = fmaxf(rmx[1], y32);
+      rmn[2] = fminf(rmn[2], z32);
+      rmx[2] = fmaxf(rmx[2], z32);
+      if (near) {
+        const double gx = p.x, gy = p.y, gz = p.z;
+        // full rotation (nn:83-85)
+        const double xa =
+            __dsub_rn(__dsub_rn(__dmul_rn(__dmul_rn(gx, cb), cl), __dmul_rn(__dmul_rn(gy, cb), sl)),
+                      __dmul_rn(gz, sb));
+        const double ya = __dadd_rn(__dmul_rn(gx, sl), __dmul_rn(gy, cl));
+        const double za =
+            __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(gx, sb), cl), __dmul_rn(__dmul_rn(gy, sb), sl)),
+                      __dmul_rn(gz, cb));
+        const unsigned long long ex = d2ord(xa), ey = d2ord(ya), ez = d2ord(za);
+        mn[0] = ex < mn[0] ? ex : mn[0];
+        mx[0] = ex > mx[0] ? ex : mx[0];
+        mn[1] = ey < mn[1] ? ey : mn[1];
+        mx[1] = ey > mx[1] ? ey : mx[1];
+        mn[2] = ez < mn[2] ? ez : mn[2];
+        mx[2] = ez > mx[2] ? ez : mx[2];
+      }
+    }
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; thomson && i < snap.n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float4 p = snap.pts[i];
     const double gx = p.x, gy = p.y, gz = p.z;
