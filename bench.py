@@ -424,12 +424,13 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                          "bytes_per_sample": bps,
-                         "kernel": "march_spectral<4,1> (first search pass + emission sums) + march_deferred "
-                                   "(the samples the first pass leaves), timed together"},
+                         "kernel": "march_spectral<4,1> (first search pass + emission sums) + march_split "
+                                   "(overflowing segments) + march_deferred (the samples the first pass "
+                                   "leaves), timed together"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            # per step: view init, view extents, view finalize, first-pass march, deferred march
-            "gpu_launches": 5 * args.steps,
+            # per step: view init, view extents, view finalize, first-pass march, overflow split, deferred march
+            "gpu_launches": 6 * args.steps,
             "serving": serving,
         }
         print(json.dumps(out))

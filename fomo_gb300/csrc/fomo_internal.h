@@ -76,8 +76,10 @@ struct LineDesc {
 };
 
 // Work counters of one march (zeroed before it): the ray queue head, the number
-// of deferred-sample records written, the deferred-record queue head.
-enum MarchCounter { kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrCount };
+// of deferred-sample records written from the front of the buffer, the
+// deferred-record queue head, the number of overflow records written from the
+// back (segments whose capsule held too many points), their queue head.
+enum MarchCounter { kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrOverflow, kCtrOverflowHead, kCtrCount };
 
 // One segment whose samples the march's first search pass could not resolve:
 // x = work item of the ray, y = first LOS sample of the segment, z/w = masks
@@ -109,7 +111,7 @@ enum MarchStat {
   kStatCandidates,     // candidates gathered
   kStatRows,           // cell rows visited by the gather
   kStatPointsLoaded,   // points loaded by the gather
-  kStatNotGathered,    // segments that fell back entirely (too many rows / candidates)
+  kStatNotGathered,    // segment parts split in halves (too many rows or candidates for one part)
   kStatFallbacks,      // samples resolved by the per-lane ring search
   kStatSamples,        // LOS samples searched
   kStatScanned,        // candidates scanned by samples

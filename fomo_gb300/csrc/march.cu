@@ -29,7 +29,9 @@
 //     FP32 distances within 4e-6) are re-ranked with the exact FP64 distance in
 //     Boost's order (dz^2 + (dy^2 + dx^2)) and the lowest original index;
 //  5. defer: every other sample (about 1 %) contributes nothing here; its
-//     segment is recorded, and a second kernel (march_deferred) searches each
+//     segment is recorded.  A segment whose capsule held more than kSegCap
+//     points is first searched again in parts of 32 or 16 samples
+//     (march_split); a third kernel (march_deferred) then searches each
 //     such sample on one lane -- rings of grid cells around the sample's cell,
 //     clipped to its box (corners rounded from FP64 as the reference does),
 //     nearest ring first, stopped by a distance bound -- then adds its emission.
@@ -252,6 +254,283 @@ __device__ __forceinline__ void clip_interval(float a, float d, float inv_d, flo
     slo = 1.0f;
     shi = 0.0f;
   }
+}
+
+struct PartIn {
+  float tx[2], ty[2], tz[2];
+  bool act[2];
+};
+struct PartOut {
+  int pos[2], orig[2];
+  bool need[2];
+};
+
+// The samples of a segment whose capsule held too many points, searched as
+// parts of `size` samples (32, then 16): each part gathers its own capsule
+// (used by march_split, off the first pass).
+__device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCtx& r, int s0, int nz, SegSmem& sm,
+                                              const PartIn in, int size) {
+  const SnapDev& S = a.snap;
+  unsigned long long* const stats = a.stats;
+  int st_rows = 0, st_loaded = 0, st_scanned = 0, st_ties = 0, st_samples = 0;
+  const int lane = threadIdx.x & 31;
+  const GridParams& g = S.g;
+  const float tx[2] = {in.tx[0], in.tx[1]}, ty[2] = {in.ty[0], in.ty[1]}, tz[2] = {in.tz[0], in.tz[1]};
+  const bool act[2] = {in.act[0], in.act[1]};
+  const int nseg = min(s0 + kSeg, nz) - s0;
+  int pos[2] = {-1, -1}, orig[2] = {-1, -1};
+  bool need0 = false, need1 = false;
+  for (int cur = 0; cur < nseg;) {
+    const int pn = min(size, nseg - cur);  // this part: samples s0 + cur .. s0 + cur + pn - 1
+    // the part's segment through its first and last targets
+    const int la = cur & 31, lb = (cur + pn - 1) & 31;
+    const bool ha = cur >= 32, hb = cur + pn - 1 >= 32;
+    float t0, t1;
+    t0 = __shfl_sync(kFull, tx[0], la); t1 = __shfl_sync(kFull, tx[1], la); const float ax = ha ? t1 : t0;
+    t0 = __shfl_sync(kFull, ty[0], la); t1 = __shfl_sync(kFull, ty[1], la); const float ay = ha ? t1 : t0;
+    t0 = __shfl_sync(kFull, tz[0], la); t1 = __shfl_sync(kFull, tz[1], la); const float az = ha ? t1 : t0;
+    t0 = __shfl_sync(kFull, tx[0], lb); t1 = __shfl_sync(kFull, tx[1], lb); const float bx = hb ? t1 : t0;
+    t0 = __shfl_sync(kFull, ty[0], lb); t1 = __shfl_sync(kFull, ty[1], lb); const float by = hb ? t1 : t0;
+    t0 = __shfl_sync(kFull, tz[0], lb); t1 = __shfl_sync(kFull, tz[1], lb); const float bz = hb ? t1 : t0;
+    const float sdx = bx - ax, sdy = by - ay, sdz = bz - az;
+    const float len2 = fmaf(sdz, sdz, fmaf(sdy, sdy, sdx * sdx));
+    const float inv_len2 = len2 > 0.0f ? 1.0f / len2 : 0.0f;
+    const float len = sqrtf(len2);
+    // local point spacing from the occupancy of the cells the part crosses
+    int occ = 0;
+    {
+      const float fs = (float)lane * (1.0f / 31.0f);
+      const float px = fmaf(fs, sdx, ax), py = fmaf(fs, sdy, ay), pz = fmaf(fs, sdz, az);
+      if (px >= g.minx && px <= g.maxx && py >= g.miny && py <= g.maxy && pz >= g.minz && pz <= g.maxz) {
+        const int c = (cell_coord(pz, g.oz, g.inv_h, g.dz) * g.dy + cell_coord(py, g.oy, g.inv_h, g.dy)) * g.dx +
+                      cell_coord(px, g.ox, g.inv_h, g.dx);
+        occ = __ldg(S.cell_start + c + 1) - __ldg(S.cell_start + c);
+      }
+    }
+    const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
+    const float aloc = g.h * cbrtf(1.0f / mocc);
+    const float R = fminf(r.mdf * 1.7321f * 1.0001f, kRScale * aloc);
+    const float amax =
+        fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
+    const float Rg = R * 1.0001f + amax * 2.4e-7f;  // + a few ulp of the coordinates
+    const float Rg2 = Rg * Rg * (1.0f + kRelPrune);
+    // ---- 1. gather
+    bool gathered = true;
+    int count = 0;
+    const float cxl = fmaxf(fminf(ax, bx) - Rg, g.minx), cxh = fminf(fmaxf(ax, bx) + Rg, g.maxx);
+    const float cyl = fmaxf(fminf(ay, by) - Rg, g.miny), cyh = fminf(fmaxf(ay, by) + Rg, g.maxy);
+    const float czl = fmaxf(fminf(az, bz) - Rg, g.minz), czh = fminf(fmaxf(az, bz) + Rg, g.maxz);
+    if (cxl <= cxh && cyl <= cyh && czl <= czh) {
+      const int x0 = cell_coord(cxl, g.ox, g.inv_h, g.dx), x1 = cell_coord(cxh, g.ox, g.inv_h, g.dx);
+      const int y0 = cell_coord(cyl, g.oy, g.inv_h, g.dy), y1 = cell_coord(cyh, g.oy, g.inv_h, g.dy);
+      const int z0 = cell_coord(czl, g.oz, g.inv_h, g.dz), z1 = cell_coord(czh, g.oz, g.inv_h, g.dz);
+      const int nyr = y1 - y0 + 1, nzr = z1 - z0 + 1;
+      const int nrows = nyr * nzr;
+      st_rows += nrows;
+      if (nrows > kMaxRows) {
+        gathered = false;
+      } else {
+        const float m = kCellMargin * g.h;
+        const float xm = Rg + m + 2e-4f * len;
+        const float inv_dy = fabsf(sdy) > 1e-30f ? 1.0f / sdy : 0.0f;
+        const float inv_dz = fabsf(sdz) > 1e-30f ? 1.0f / sdz : 0.0f;
+        const unsigned lt = (1u << lane) - 1u;
+        for (int rb = 0; rb < nrows && count <= kSegCap; rb += 32) {
+          const int rr = rb + lane;
+          int n = 0, base = 0;
+          if (rr < nrows) {
+            const int jy = y0 + rr % nyr, kz = z0 + rr / nyr;
+            float slo = 0.0f, shi = 1.0f;
+            clip_interval(ay, sdy, inv_dy, fmaf((float)jy, g.h, g.oy) - m - Rg,
+                          fmaf((float)(jy + 1), g.h, g.oy) + m + Rg, slo, shi);
+            clip_interval(az, sdz, inv_dz, fmaf((float)kz, g.h, g.oz) - m - Rg,
+                          fmaf((float)(kz + 1), g.h, g.oz) + m + Rg, slo, shi);
+            slo = fmaxf(slo, 0.0f);
+            shi = fminf(shi, 1.0f);
+            if (slo <= shi) {
+              const float xa = fmaf(slo, sdx, ax), xb = fmaf(shi, sdx, ax);
+              const int c0 = max(x0, cell_coord(fminf(xa, xb) - xm, g.ox, g.inv_h, g.dx));
+              const int c1 = min(x1, cell_coord(fmaxf(xa, xb) + xm, g.ox, g.inv_h, g.dx));
+              if (c0 <= c1) {
+                const int rowbase = (kz * g.dy + jy) * g.dx;
+                base = __ldg(S.cell_start + rowbase + c0);
+                n = __ldg(S.cell_start + rowbase + c1 + 1) - base;
+              }
+            }
+          }
+          // rows' point ranges, prefix-summed across the warp and loaded 32 at a time
+          const int incl = warp_incl_scan(n);
+          const int excl = incl - n;
+          const int total = __shfl_sync(kFull, incl, 31);
+          st_loaded += total;
+          for (int ib = 0; ib < total; ib += 32) {
+            const int i = ib + lane;
+            const int own = warp_owner(incl, i);
+            const int ob = __shfl_sync(kFull, base, own);
+            const int oe = __shfl_sync(kFull, excl, own);
+            bool keep = false;
+            float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+            int p = 0, bk = 0;
+            if (i < total) {
+              p = ob + (i - oe);
+              q = __ldg(S.pts + p);
+              const float wx = q.x - ax, wy = q.y - ay, wz = q.z - az;
+              float s = fmaf(wz, sdz, fmaf(wy, sdy, wx * sdx)) * inv_len2;
+              s = fminf(fmaxf(s, 0.0f), 1.0f);
+              const float ex = fmaf(-s, sdx, wx), ey = fmaf(-s, sdy, wy), ez = fmaf(-s, sdz, wz);
+              keep = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) <= Rg2;
+              bk = min(max(__float2int_rn(s * (float)(pn - 1)), 0), pn - 1);
+            }
+            const unsigned msk = __ballot_sync(kFull, keep);
+            if (keep) {
+              const int slot = count + __popc(msk & lt);
+              if (slot < kSegCap) {
+                sm.q[slot] = q;
+                sm.pos[slot] = p;
+                sm.cb[slot] = (unsigned char)bk;
+              }
+            }
+            count += __popc(msk);
+          }
+        }
+        if (count > kSegCap) gathered = false;
+      }
+    }
+    if (stats && lane == 0) atomicAdd(stats + kStatCandidates, (unsigned long long)count);
+    if (!gathered && pn > 16) {
+      // too many points for one part: the same samples again as two halves
+      if (stats && lane == 0) atomicAdd(stats + kStatNotGathered, 1ull);
+      size = pn >> 1;
+      continue;
+    }
+    const int ncand = gathered ? count : 0;
+    // ---- 2. counting sort by sample index
+    sm.cursor[lane] = 0;
+    sm.cursor[lane + 32] = 0;
+    __syncwarp();
+    for (int c = lane; c < ncand; c += 32) atomicAdd(&sm.cursor[sm.cb[c]], 1);
+    __syncwarp();
+    {
+      const int h0 = sm.cursor[2 * lane], h1 = sm.cursor[2 * lane + 1];
+      const int incl = warp_incl_scan(h0 + h1);
+      const int ex = incl - h0 - h1;
+      __syncwarp();
+      sm.bstart[2 * lane] = ex;
+      sm.bstart[2 * lane + 1] = ex + h0;
+      if (lane == 31) sm.bstart[kSeg] = incl;
+      sm.cursor[2 * lane] = ex;
+      sm.cursor[2 * lane + 1] = ex + h0;
+    }
+    __syncwarp();
+    for (int c = lane; c < ncand; c += 32) {
+      const int dst = kSegCap + atomicAdd(&sm.cursor[sm.cb[c]], 1);
+      sm.q[dst] = sm.q[c];
+      sm.pos[dst] = sm.pos[c];
+    }
+    __syncwarp();
+    const float4* sq = sm.q + kSegCap;  // the candidates in sample order
+    const int* spos = sm.pos + kSegCap;
+    // ---- 3./4. per-sample scan of the buckets within R, acceptance
+    const float dlt = (pn > 1) ? len / (float)(pn - 1) : 0.0f;
+    const int w = (dlt > 0.0f) ? min((int)(Rg / dlt + 0.51f) + 1, kSeg) : kSeg;
+#pragma unroll 1
+    for (int i = 0; i < 2; ++i) {
+      // one copy of the scan code for both samples of the lane (instruction cache)
+      const int j = lane + 32 * i - cur;  // bucket of this lane's sample in the part
+      const bool acti = (i ? act[1] : act[0]) && j >= 0 && j < pn;
+      if (!acti) continue;
+      int pres = -1, ores = -1;
+      bool accept = false;
+      if (gathered) {
+        const int c0 = sm.bstart[max(j - w, 0)], c1 = sm.bstart[min(j + w, pn - 1) + 1];
+        st_scanned += c1 - c0;
+        const float t_x = i ? tx[1] : tx[0], t_y = i ? ty[1] : ty[0], t_z = i ? tz[1] : tz[0];
+        const float tmax = fmaxf(fmaxf(fabsf(t_x), fabsf(t_y)), fabsf(t_z));
+        const float delta = (tmax + r.mdf) * 4.8e-7f + r.mdf * 1.2e-7f;  // ~4 ulp of the box corners
+        const float md_in = r.mdf - delta, md_out = r.mdf + delta;
+        float b1 = FLT_MAX, b2 = FLT_MAX;
+        int bi = -1;
+        bool amb = false;
+        for (int c = c0; c < c1; ++c) {
+          const float4 q = sq[c];
+          const float dx = q.x - t_x, dy = q.y - t_y, dz = q.z - t_z;
+          const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          const float cheb = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+          if (cheb < md_in) {
+            if (d2 < b1) {
+              b2 = b1;
+              b1 = d2;
+              bi = c;
+            } else if (d2 < b2) {
+              b2 = d2;
+            }
+          } else if (cheb <= md_out) {
+            amb = true;
+          }
+        }
+        // coverage: every point within cov of the target was gathered
+        const float wx = t_x - ax, wy = t_y - ay, wz = t_z - az;
+        float s = fmaf(wz, sdz, fmaf(wy, sdy, wx * sdx)) * inv_len2;
+        s = fminf(fmaxf(s, 0.0f), 1.0f);
+        const float ex = fmaf(-s, sdx, wx), ey = fmaf(-s, sdy, wy), ez = fmaf(-s, sdz, wz);
+        const float cov = Rg - sqrtf(fmaf(ez, ez, fmaf(ey, ey, ex * ex))) - amax * 2.4e-7f;
+        if (!amb && cov > 0.0f) {
+          if (bi >= 0)
+            accept = b1 < cov * cov * (1.0f - 2.0f * kRelPrune);
+          else
+            accept = md_out * 1.7321f * 1.0001f < cov;  // the whole box lies inside the gathered ball
+        }
+        if (!accept && bi < 0 && !amb) {
+          // no candidate: the box is empty for sure when it lies outside the
+          // points' bounding box (hi <= min or lo >= max on some axis)
+          accept = (t_x + md_out <= g.minx) || (t_x - md_out >= g.maxx) || (t_y + md_out <= g.miny) ||
+                   (t_y - md_out >= g.maxy) || (t_z + md_out <= g.minz) || (t_z - md_out >= g.maxz);
+        }
+        if (accept && bi >= 0) {
+          if (b2 <= b1 * (1.0f + kRelTie)) {
+            // possible FP64 tie: exact re-rank of the in-box contenders
+            ++st_ties;
+            bi = exact_rerank_list(sq, c0, c1, t_x, t_y, t_z, md_in, b1 * (1.0f + kRelTie));
+          }
+          pres = spos[bi];
+          ores = __float_as_int(sq[bi].w);
+        }
+        if (stats && !accept)  // rare: counted where it happens
+          atomicAdd(stats + (amb ? kStatFbAmb : (bi < 0 ? kStatFbNoCand : kStatFbFar)), 1ull);
+      }
+      ++st_samples;
+      if (i) {
+        pos[1] = pres;
+        orig[1] = ores;
+        need1 = !accept;
+      } else {
+        pos[0] = pres;
+        orig[0] = ores;
+        need0 = !accept;
+      }
+    }
+    __syncwarp();  // the candidate lists are rewritten by the next part
+    cur += pn;
+  }
+  if (stats) {
+    const unsigned sc = __reduce_add_sync(kFull, (unsigned)st_scanned);
+    const unsigned ti = __reduce_add_sync(kFull, (unsigned)st_ties);
+    if (lane == 0) {
+      atomicAdd(stats + kStatRows, (unsigned long long)st_rows);
+      atomicAdd(stats + kStatPointsLoaded, (unsigned long long)st_loaded);
+      atomicAdd(stats + kStatScanned, (unsigned long long)sc);
+      atomicAdd(stats + kStatTies, (unsigned long long)ti);
+    }
+  }
+  (void)st_samples;
+  PartOut o;
+  o.pos[0] = pos[0];
+  o.pos[1] = pos[1];
+  o.orig[0] = orig[0];
+  o.orig[1] = orig[1];
+  o.need[0] = need0;
+  o.need[1] = need1;
+  return o;
 }
 
 // Warp-collective: nearest neighbours of the segment's samples s0 .. s0+63.
@@ -505,8 +784,12 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
   // here and deferred to the second kernel: one record per segment
   const unsigned f0 = __ballot_sync(kFull, need0), f1 = __ballot_sync(kFull, need1);
   if ((f0 | f1) && lane == 0) {
-    const unsigned long long slot = atomicAdd(a.counter + kCtrDeferred, 1ull);
-    if ((int64_t)slot < a.deferred_cap)  // always: the capacity is one record per segment
+    // a segment whose capsule held too many points is queued from the back,
+    // for march_split to search in parts; the others from the front
+    const bool over = !gathered && nseg > 16;
+    const unsigned long long k = atomicAdd(a.counter + (over ? kCtrOverflow : kCtrDeferred), 1ull);
+    const int64_t slot = over ? a.deferred_cap - 1 - (int64_t)k : (int64_t)k;
+    if (slot >= 0 && slot < a.deferred_cap)  // always: the capacity is one record per segment
       a.deferred[slot] = make_uint4(r.item, (unsigned)s0, f0, f1);
   }
   if (stats) {
@@ -900,13 +1183,144 @@ __device__ __forceinline__ int nth_set_bit(unsigned lo, unsigned hi, int n) {
   return 32 + (int)__fns(hi, 0, n - nlo + 1);
 }
 
+// Warp-collective: adds the emission of n samples of ray r, whose neighbours
+// (sorted positions, -1 for none) and LOS speeds are sp[0..n) and sv[0..n) in
+// shared memory, to the ray's outputs with atomics.  Spectral: lane = lambda
+// bin of each line window; imaging and Thomson: a warp sum per line.
+__device__ __forceinline__ void add_emission(const MarchArgs& a, const RayCtx& r, int kind, const int* sp,
+                                             const float* sv, int n) {
+  const int lane = threadIdx.x & 31;
+  const ViewDesc* V = a.views + r.v;
+  const int64_t ray = (int64_t)r.i * V->nx + r.j;
+  const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
+  if (kind == kDeferredSpectral) {
+    const int L = V->L;
+    for (int l = 0; l < a.nlines; ++l) {
+      const LineDesc& D = LD[l];
+      if (!D.ew) continue;  // views may have fewer lines than the launch
+      const double scale = D.is_dn ? V->scale_dn : V->scale;
+      for (int m = 0; m < D.nw; ++m) {
+        const int il = D.wstart + 32 * m + lane;
+        const float lamv = il < L ? __ldg(D.lam + il) : 3.0e30f;
+        float part = 0.0f;
+        for (int f = 0; f < n; ++f) {
+          const int p = sp[f];
+          if (p < 0) continue;
+          const float2 pw = __ldg(D.ew + p);
+          if (pw.x == 0.0f) continue;  // intpolpeak ? ... : 0 (nn:204)
+          const float sc = __fdividef(2.0f, pw.y);
+          const float ns = -(sv[f] * D.shift_k) * sc;
+          const float q = fmaf(lamv, sc, ns);
+          part = fmaf(pw.x, ex2_approx(-q * q), part);
+        }
+        if (il < L && part != 0.0f) atomicAdd(D.out + ray * L + il, __double2float_rn(__dmul_rn(scale, (double)part)));
+      }
+    }
+  } else {
+    const float* s2v = kind == kDeferredThomson ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
+    for (int l = 0; l < a.nlines; ++l) {
+      const LineDesc& D = LD[l];
+      if (!D.out) continue;
+      float val = 0.0f;
+      for (int f = lane; f < n; f += 32) {
+        const int p = sp[f];
+        if (p >= 0) val += s2v ? fmaxf(__ldg(a.totpol + p).y * __ldg(s2v + p), 0.0f) : __ldg(D.ew + p).x;
+      }
+      const float sum = warp_sum(val);
+      if (lane == 0 && sum != 0.0f)
+        atomicAdd(D.out + ray, __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
+    }
+  }
+}
+
+// The record at position ri of the deferred queue: the first pass's records
+// from the front of the buffer, then the overflow records from the back.
+__device__ __forceinline__ DeferredRec deferred_at(const MarchArgs& a, int64_t nfront, int64_t ri) {
+  return ri < nfront ? a.deferred[ri] : a.deferred[a.deferred_cap - 1 - (ri - nfront)];
+}
+
+// ---------------------------------------------------------------------------
+// Overflow segments: a segment whose capsule held more than kSegCap points
+// (dense clumps, long segments at a coarse LOS step) is queued by the first
+// pass at the back of the deferred buffer with all its samples.  This kernel
+// searches each such segment again as parts of 32 samples (16 when a part
+// overflows too), each part gathering its own, shorter capsule, adds the
+// emission of the samples it resolves and rewrites the record with the
+// samples still unresolved, for march_deferred.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, kMinCtas) march_split(MarchArgs a, const double3* __restrict__ ktab,
+                                                        int ktab_stride, int kind) {
+  __shared__ SegSmem segs[kWarps];
+  __shared__ int spos[kWarps][kSeg];
+  __shared__ float svlos[kWarps][kSeg];
+  const int w = threadIdx.x >> 5;
+  SegSmem& sm = segs[w];
+  const int lane = threadIdx.x & 31;
+  const int64_t nover = min((int64_t)a.counter[kCtrOverflow], a.deferred_cap);  // written by the march
+  for (;;) {
+    unsigned long long k = 0;
+    if (lane == 0) k = atomicAdd(a.counter + kCtrOverflowHead, 1ull);
+    k = __shfl_sync(kFull, k, 0);
+    if ((int64_t)k >= nover) return;
+    const int64_t slot = a.deferred_cap - 1 - (int64_t)k;
+    const DeferredRec rec = a.deferred[slot];
+    RayCtx r;
+    if (!ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, r)) continue;  // records come from real rays only
+    const ViewDesc* V = a.views + r.v;
+    const int nz = V->nz, s0 = (int)rec.y;
+    PartIn in;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int kk = s0 + lane + 32 * i;
+      in.act[i] = kk < nz && (((i ? rec.w : rec.z) >> lane) & 1u);
+      double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+      if (kk < nz) sample_pos(r, kk, p0, p1, p2);
+      in.tx[i] = __double2float_rn(p0);  // the FP32 target (nn:171)
+      in.ty[i] = __double2float_rn(p1);
+      in.tz[i] = __double2float_rn(p2);
+    }
+    const PartOut o = segment_parts(a, r, s0, nz, sm, in, 32);
+    // resolved samples: NN index, then the emission of those with a neighbour
+    int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+    const int64_t ray = (int64_t)r.i * V->nx + r.j;
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const bool done = in.act[i] && !o.need[i];
+      if (nnout && done) nnout[ray * nz + s0 + lane + 32 * i] = o.orig[i];
+      const bool fill = done && o.pos[i] >= 0;
+      const unsigned fm = __ballot_sync(kFull, fill);
+      if (fill) {
+        const int d = n + __popc(fm & ((1u << lane) - 1u));
+        float vl = 0.0f;
+        if (kind == kDeferredSpectral) {
+          const float4 vv = __ldg(a.snap.vel + o.pos[i]);
+          vl = fmaf(V->uz, vv.z, fmaf(V->uy, vv.y, V->ux * vv.x));
+        }
+        spos[w][d] = o.pos[i];
+        svlos[w][d] = vl;
+      }
+      n += __popc(fm);
+    }
+    __syncwarp();
+    if (n > 0) add_emission(a, r, kind, spos[w], svlos[w], n);
+    __syncwarp();  // the staging arrays are rewritten by the next record
+    const unsigned f0 = __ballot_sync(kFull, in.act[0] && o.need[0]);
+    const unsigned f1 = __ballot_sync(kFull, in.act[1] && o.need[1]);
+    if (lane == 0) a.deferred[slot] = make_uint4(rec.x, rec.y, f0, f1);
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride, int kind) {
   __shared__ int spos[kWarps][kDefBatch];    // neighbour (sorted position) of each staged sample
   __shared__ float svlos[kWarps][kDefBatch]; // and its LOS speed (spectral)
   const int w = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int64_t nrec = min((int64_t)a.counter[kCtrDeferred], a.deferred_cap);  // written by the march
+  // written by the march and march_split; the two ends of the buffer never meet
+  // (at most one record per segment)
+  const int64_t nfront = min((int64_t)a.counter[kCtrDeferred], a.deferred_cap);
+  const int64_t nrec = nfront + min((int64_t)a.counter[kCtrOverflow], a.deferred_cap - nfront);
   for (;;) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(a.counter + kCtrDeferredHead, 32ull);
@@ -914,7 +1328,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
     if ((int64_t)base >= nrec) return;
     const int64_t ri = (int64_t)base + lane;
     DeferredRec rec = make_uint4(0u, 0u, 0u, 0u);
-    if (ri < nrec) rec = a.deferred[ri];
+    if (ri < nrec) rec = deferred_at(a, nfront, ri);
     const int cnt = __popc(rec.z) + __popc(rec.w);
     const int incl = warp_incl_scan(cnt);
     const int excl = incl - cnt;
@@ -959,49 +1373,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
         const int sn = __shfl_sync(kFull, cnt, rr);
         const int so = __shfl_sync(kFull, excl, rr) - start;
         const RayCtx r = shfl_ray(mine, rr);
-        if (sn == 0) continue;
-        const ViewDesc* V = a.views + r.v;
-        const int64_t ray = (int64_t)r.i * V->nx + r.j;
-        const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
-        if (kind == kDeferredSpectral) {
-          const int L = V->L;
-          for (int l = 0; l < a.nlines; ++l) {
-            const LineDesc& D = LD[l];
-            if (!D.ew) continue;  // views may have fewer lines than the launch
-            const double scale = D.is_dn ? V->scale_dn : V->scale;
-            for (int m = 0; m < D.nw; ++m) {
-              const int il = D.wstart + 32 * m + lane;
-              const float lamv = il < L ? __ldg(D.lam + il) : 3.0e30f;
-              float part = 0.0f;
-              for (int f = so; f < so + sn; ++f) {
-                const int p = spos[w][f];
-                if (p < 0) continue;
-                const float2 pw = __ldg(D.ew + p);
-                if (pw.x == 0.0f) continue;  // intpolpeak ? ... : 0 (nn:204)
-                const float sc = __fdividef(2.0f, pw.y);
-                const float ns = -(svlos[w][f] * D.shift_k) * sc;
-                const float q = fmaf(lamv, sc, ns);
-                part = fmaf(pw.x, ex2_approx(-q * q), part);
-              }
-              if (il < L && part != 0.0f)
-                atomicAdd(D.out + ray * L + il, __double2float_rn(__dmul_rn(scale, (double)part)));
-            }
-          }
-        } else {
-          const float* s2v = kind == kDeferredThomson ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
-          for (int l = 0; l < a.nlines; ++l) {
-            const LineDesc& D = LD[l];
-            if (!D.out) continue;
-            float val = 0.0f;
-            for (int f = so + lane; f < so + sn; f += 32) {
-              const int p = spos[w][f];
-              if (p >= 0) val += s2v ? fmaxf(__ldg(a.totpol + p).y * __ldg(s2v + p), 0.0f) : __ldg(D.ew + p).x;
-            }
-            const float sum = warp_sum(val);
-            if (lane == 0 && sum != 0.0f)
-              atomicAdd(D.out + ray, __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
-          }
-        }
+        if (sn > 0) add_emission(a, r, kind, spos[w] + so, svlos[w] + so, sn);
       }
       __syncwarp();  // the staging arrays are rewritten by the next batch
       r0 = r1;
@@ -1034,6 +1406,16 @@ cudaError_t launch_deferred(const MarchArgs& a, const double3* ktab, int ktab_st
   // the record count is known on the device only: a persistent grid that
   // drains the queue (and exits at once when it is empty)
   march_deferred<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split(const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count, cudaStream_t s,
+                         int kind) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_split, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  march_split<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
   return cudaGetLastError();
 }
 
@@ -1079,6 +1461,8 @@ cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_strid
   cudaError_t e = launch_first_pass(a, ktab, ktab_stride, max_windows, sm_count, s, blocks_per_sm_hint, imaging);
   if (e != cudaSuccess) return e;
   const int kind = a.s2 ? kDeferredThomson : (imaging ? kDeferredImaging : kDeferredSpectral);
+  e = launch_split(a, ktab, ktab_stride, sm_count, s, kind);
+  if (e != cudaSuccess) return e;
   return launch_deferred(a, ktab, ktab_stride, sm_count, s, kind);
 }
 
