@@ -795,6 +795,17 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
       }
     }
     G.total_items = hoff[G.nv];
+    G.item_off.assign(hoff, hoff + G.nv + 1);
+    G.vcost.assign(G.nv, 0.0);
+    G.out_bytes = 0;
+    for (int v = 0; v < G.nv; ++v) {
+      const fomo_request& q0 = reqs[G.vreqs[v][0]];
+      G.vcost[v] = (double)q0.nx * q0.ny * q0.nz;
+      for (int r : G.vreqs[v]) {
+        G.vcost[v] += (double)cube_elems(reqs[r]);
+        G.out_bytes += cube_elems(reqs[r]) * sizeof(float);
+      }
+    }
     G.max_nw = 1;
     for (int v = 0; v < G.nv; ++v)
       for (int li = 0; li < (int)G.vreqs[v].size(); ++li) G.max_nw = std::max(G.max_nw, hl[(size_t)v * G.nl + li].nw);
@@ -808,7 +819,24 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
 
 // Enqueue a planned batch on stream s: one descriptor upload, then per launch
 // view set-up and the persistent march.
-int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s) {
+// Cut points [0 = c0 < c1 < ... = nv] of the view ranges a launch marches in
+// when its cubes download as they complete: about equal shares of the views'
+// cost, one range per 256 MB of cubes, 8 at most.
+static std::vector<int> view_ranges(const PlanGroup& G, bool split) {
+  const size_t n = split ? std::min<size_t>({8, (size_t)G.nv, std::max<size_t>(1, G.out_bytes >> 28)}) : 1;
+  double total = 0.0;
+  for (double c : G.vcost) total += c;
+  std::vector<int> cuts{0};
+  double acc = 0.0;
+  for (int v = 0; v < G.nv; ++v) {
+    if (v > cuts.back() && cuts.size() < n && acc >= total * (double)cuts.size() / (double)n) cuts.push_back(v);
+    acc += G.vcost[v];
+  }
+  cuts.push_back(G.nv);
+  return cuts;
+}
+
+int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done) {
   char* db = scr->arena.base;
   // Under stream capture an ordinary event record is only a capture-internal
   // dependency: the staging event is then recorded after the graph launch,
@@ -850,14 +878,27 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s)
     a.totpol = G.totpol;
     a.stats = ctx->march_stats;
     if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = record_timing(scr->ev0);
+    int rc = FOMO_OK;
     if (G.method == FOMO_METHOD_PROJECTION) {
       for (const auto& z : G.zero_outs)
         if (e == cudaSuccess) e = cudaMemsetAsync(z.first, 0, z.second, s);
       if (e == cudaSuccess) e = launch_projection(sd, dv, a.lines, G.nv, G.nl, G.imaging, ctx->sm_count, s);
+      if (e == cudaSuccess && done) rc = (*done)(G, 0, G.nv);
     } else if (e == cudaSuccess) {
-      e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
-                       G.method == FOMO_METHOD_THOMSON || G.imaging);
+      // the march over view ranges: each range's rays are a contiguous run of
+      // work items, with the work counters cleared before it
+      const std::vector<int> cuts = view_ranges(G, done != nullptr);
+      for (size_t k = 0; k + 1 < cuts.size() && e == cudaSuccess && rc == FOMO_OK; ++k) {
+        if (k > 0) e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * kCtrCount, s);
+        a.item_base = G.item_off[cuts[k]];
+        a.total_items = G.item_off[cuts[k + 1]];
+        if (e == cudaSuccess)
+          e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
+                           G.method == FOMO_METHOD_THOMSON || G.imaging);
+        if (e == cudaSuccess && done) rc = (*done)(G, cuts[k], cuts[k + 1]);
+      }
     }
+    if (rc) return rc;
     if (e == cudaSuccess && scr->ev1 && ctx->time_march) e = record_timing(scr->ev1);
   }
   if (e != cudaSuccess) return cuda_err(ctx, e, "render launch");
@@ -865,13 +906,14 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s)
 }
 
 int enqueue_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
-                  cudaStream_t s, std::vector<ViewDesc>* views_out, std::vector<int>* view_of_req) {
+                  cudaStream_t s, std::vector<ViewDesc>* views_out, std::vector<int>* view_of_req,
+                  const RangeDone* done) {
   Plan plan;
   int rc = plan_batch(ctx, reqs, nreq, d_out, d_nn, &ctx->scratch, &plan);
   if (rc) return rc;
   rc = order_streams(ctx, s);
   if (rc) return rc;
-  rc = issue_plan(ctx, plan, &ctx->scratch, s);
+  rc = issue_plan(ctx, plan, &ctx->scratch, s, done);
   if (rc) return rc;
   if (view_of_req) *view_of_req = plan.view_of_req;
   if (views_out) {
@@ -982,6 +1024,11 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
     cudaFree(ctx->march_stats);
   }
   ctx->scratch.release();
+  for (cudaEvent_t ev : ctx->range_ev) cudaEventDestroy(ev);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
   cudaEventDestroy(ctx->order_ev);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -1209,16 +1256,44 @@ int fomo_render_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* 
   }
   int rc = ctx->out_arena.reserve(ctx, total);
   if (rc) return rc;
+  if (!ctx->copy_stream) FOMO_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "copy stream");
   std::vector<float*> d(nreq);
   for (int r = 0; r < nreq; ++r) d[r] = reinterpret_cast<float*>(ctx->out_arena.base + off[r]);
+  // The cubes of each range of views download on the copy stream while the
+  // next range marches.  A range's downloads are issued after the next
+  // range's march is queued: into pageable memory they return only when done.
+  std::vector<int> pending;  // requests of the range before
+  size_t nev = 0;
+  auto download = [&](const std::vector<int>& rs) -> int {
+    for (int r : rs)
+      FOMO_CUDA(cudaMemcpyAsync(outs[r], d[r], cube_elems(reqs[r]) * sizeof(float), cudaMemcpyDeviceToHost,
+                                ctx->copy_stream),
+                "cube download");
+    return FOMO_OK;
+  };
+  RangeDone done = [&](const PlanGroup& G, int v0, int v1) -> int {
+    if (nev == ctx->range_ev.size()) {
+      cudaEvent_t ev = nullptr;
+      FOMO_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "range event");
+      ctx->range_ev.push_back(ev);
+    }
+    const cudaEvent_t ev = ctx->range_ev[nev++];
+    FOMO_CUDA(cudaEventRecord(ev, ctx->stream), "range event");
+    int rc2 = download(pending);
+    pending.clear();
+    FOMO_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ev, 0), "range wait");
+    for (int v = v0; v < v1; ++v) pending.insert(pending.end(), G.vreqs[v].begin(), G.vreqs[v].end());
+    return rc2;
+  };
   std::vector<ViewDesc> views;
   std::vector<int> vof;
-  rc = enqueue_batch(ctx, reqs, nreq, d.data(), nullptr, ctx->stream, infos ? &views : nullptr, &vof);
+  rc = enqueue_batch(ctx, reqs, nreq, d.data(), nullptr, ctx->stream, infos ? &views : nullptr, &vof, &done);
+  if (rc == FOMO_OK) rc = download(pending);
+  // the caller's buffers must not be written after return, error or not
+  const cudaError_t e1 = cudaStreamSynchronize(ctx->copy_stream);
+  const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
   if (rc) return rc;
-  for (int r = 0; r < nreq; ++r)
-    FOMO_CUDA(cudaMemcpyAsync(outs[r], d[r], cube_elems(reqs[r]) * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
-              "cube download");
-  FOMO_CUDA(cudaStreamSynchronize(ctx->stream), "render");
+  FOMO_CUDA(e1 != cudaSuccess ? e1 : e2, "render");
   if (ctx->time_march) cudaEventElapsedTime(&ctx->last_ms, ctx->scratch.ev0, ctx->scratch.ev1);
   if (infos) {
     rc = finish_views(ctx, &views);

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
 #include <string>
 #include <tuple>
@@ -98,6 +99,9 @@ struct PlanGroup {
   size_t o_def = 0;          // deferred-sample records
   std::vector<std::pair<float*, size_t>> zero_outs;  // projection outputs to clear before the scatter
   int64_t deferred_cap = 0;  // records: one per segment of every work item
+  std::vector<int64_t> item_off;  // first work item of each view (nv + 1 entries)
+  std::vector<double> vcost;      // LOS samples + output cells of each view
+  size_t out_bytes = 0;           // cube bytes of all its requests
 };
 
 struct Plan {
@@ -147,6 +151,10 @@ struct fomo_ctx {
   bool time_march = true;
   float last_ms = 0.0f;
   cudaEvent_t order_ev = nullptr;  // orders a caller stream after the context stream
+  // host-output batches: the cube downloads of one range of views overlap the
+  // march of the next (created on first use)
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> range_ev;
   std::map<std::string, fomo::GraphRec> graphs;
   std::map<std::string, fomo::TuneChoice> tuned;
 };
@@ -159,11 +167,16 @@ int dev_alloc(fomo_ctx* ctx, void** p, size_t bytes);
 void dev_free(fomo_ctx* ctx, void* p);
 int validate(fomo_ctx* ctx, const fomo_request& q);
 size_t cube_elems(const fomo_request& q);
+// Called by issue_plan once the work of views [v0, v1) of launch G is on the
+// stream: their cubes are complete when the stream reaches that point.  With
+// it, a large launch marches in up to 8 view ranges (one per 256 MB of cubes).
+using RangeDone = std::function<int(const PlanGroup& G, int v0, int v1)>;
 int enqueue_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
-                  cudaStream_t s, std::vector<ViewDesc>* views_out, std::vector<int>* view_of_req);
+                  cudaStream_t s, std::vector<ViewDesc>* views_out, std::vector<int>* view_of_req,
+                  const RangeDone* done = nullptr);
 int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
                ScratchSet* scr, Plan* plan);
-int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s);
+int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done = nullptr);
 std::string workload_class(const PlanGroup& G, const SnapRec& snap);
 int order_streams(fomo_ctx* ctx, cudaStream_t s);
 SnapDev snap_dev(const SnapRec& r);

@@ -58,6 +58,29 @@ def test_graph_replay_equals_direct(ctx):
     ctx.drop_snapshot(sid)
 
 
+def test_host_batch_downloads_in_chunks_same_as_alone(ctx):
+    """About 1 GB of cubes: the batch marches in four chunks of views whose
+    cubes download while the next chunk marches.  Every cube and view info must
+    match the same request rendered alone, with lines of one view kept together
+    even when the caller interleaves them."""
+    s = synth.loop_snapshot(24, seed=21)
+    sid = ctx.snapshot(s)
+    tids = [ctx.table(synth.line_table(peak_logT=p, lambda0=lam)) for p, lam in ((5.9, 171.0), (6.2, 211.0))]
+    bb = ctx.table(synth.broadband_table(171))
+    views = [(0.15 * k, 0.05 * (k - 4)) for k in range(9)]
+    reqs = []
+    for tid in tids:  # line-major order: a view's two lines are far apart in the list
+        for (l, b) in views:
+            reqs.append(ctx.request(sid, tid, fg.METHOD_NN, 512, 512, 32, 64, l, b, 1.5e5))
+    reqs.append(ctx.request(sid, bb, fg.METHOD_NN, 256, 128, 40, 1, 0.7, 0.2, 1e5))
+    cubes, infos = ctx.render_batch(reqs)
+    for q, c, inf in zip(reqs, cubes, infos):
+        single, _, sinf = ctx.render(q)
+        assert G.norm_max_err(c.ravel(), single.ravel()) <= 1e-6
+        assert inf.as_dict() == sinf.as_dict()
+    ctx.drop_snapshot(sid)
+
+
 def test_server_same_alone_and_in_mix():
     rng = np.random.default_rng(17)
     with fg.Server(0) as srv:
