@@ -78,8 +78,11 @@ struct LineDesc {
 // Work counters of one march (zeroed before it): the ray queue head, the number
 // of deferred-sample records written from the front of the buffer, the
 // deferred-record queue head, the number of overflow records written from the
-// back (segments whose capsule held too many points), their queue head.
-enum MarchCounter { kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrOverflow, kCtrOverflowHead, kCtrCount };
+// back (segments whose capsule held too many points), their queue head, the
+// number of hard samples queued for a warp each, their queue head.
+enum MarchCounter {
+  kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrOverflow, kCtrOverflowHead, kCtrHard, kCtrHardHead, kCtrCount
+};
 
 // One segment whose samples the march's first search pass could not resolve:
 // x = work item of the ray, y = first LOS sample of the segment, z/w = masks
@@ -98,6 +101,8 @@ struct MarchArgs {
   unsigned long long* counter;   // kCtrCount work counters, zeroed before the launch
   DeferredRec* deferred;         // one record per segment at most: capacity deferred_cap
   int64_t deferred_cap;
+  uint2* hard;                   // deferred samples (work item, sample) for a whole warp each, or null
+  int64_t hard_cap;              // its capacity (0: every deferred sample is searched by one lane)
   int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
@@ -119,8 +124,9 @@ enum MarchStat {
   kStatFbNoCand,       // fallback reason: no in-box candidate within the coverage radius
   kStatFbFar,          // fallback reason: best candidate beyond the coverage radius
   kStatFbAmb,          // fallback reason: a candidate within a few ulp of a box face
-  kStatFbUnion,        // fallback samples resolved by the union-of-boxes gather
+  kStatFbUnion,        // samples searched by the deferred pass
   kStatDeferredRecs,   // deferred-sample records (segments with fallback samples)
+  kStatHard,           // deferred samples whose one-lane search ran out of budget (searched by a warp)
   kStatCount
 };
 
@@ -178,5 +184,11 @@ cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_strid
 int march_bins_per_lane(int nlines, int L);
 // Capacity of the deferred-record queue for `items` work items of up to nz samples.
 inline int64_t deferred_capacity(int64_t items, int nz) { return items * ((nz + 63) / 64); }
+// Hard-sample queue of a launch: up to 2^20 entries (8 MB); when it is full a
+// lane finishes its search on its own.
+inline int64_t hard_capacity(int64_t items, int nz) {
+  const int64_t n = items * (int64_t)nz;
+  return n < (int64_t(1) << 20) ? n : (int64_t(1) << 20);
+}
 
 }  // namespace fomo

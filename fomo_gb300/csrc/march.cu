@@ -1020,37 +1020,44 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_imaging(MarchArgs a,
 enum DeferredKind : int { kDeferredSpectral = 0, kDeferredImaging = 1, kDeferredThomson = 2 };
 constexpr int kDefBatch = 256;  // deferred samples staged per warp between search and contribution
 
-// Candidates p in [p0, p1) inside box q: the two best FP32 squared distances,
-// or (EXACT) the smallest FP64 distance within `band`, lowest original index
-// on exact ties.
+// Candidate v (sorted position p) against box q: kept when strictly inside;
+// the two best FP32 squared distances, or (EXACT) the smallest FP64 distance
+// within `band`, lowest original index on exact ties.
 template <bool EXACT>
-__device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p0, int p1, float band, float& best,
-                                          float& second, int& bpos, int& borig, double& bD) {
-  for (int p = p0; p < p1; ++p) {
-    const float4 v = __ldg(S.pts + p);
-    if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-      const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-      const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      const int o = __float_as_int(v.w);
-      if (!EXACT) {
-        if (d < best) {
-          second = best;
-          best = d;
-          bpos = p;
-          borig = o;
-        } else if (d < second) {
-          second = d;
-        }
-      } else if (d <= band) {
-        const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
-        if (D < bD || (D == bD && o < borig)) {
-          bD = D;
-          borig = o;
-          bpos = p;
-        }
+__device__ __forceinline__ void scan_point(const float4 v, int p, const BoxQ& q, float band, float& best,
+                                           float& second, int& bpos, int& borig, double& bD) {
+  if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+    const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+    const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const int o = __float_as_int(v.w);
+    if (!EXACT) {
+      if (d < best) {
+        second = best;
+        best = d;
+        bpos = p;
+        borig = o;
+      } else if (d < second) {
+        second = d;
+      }
+    } else if (d <= band) {
+      const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
+      if (D < bD || (D == bD && o < borig)) {
+        bD = D;
+        borig = o;
+        bpos = p;
       }
     }
   }
+}
+
+// Candidates p in [p0, p1), one after the other; `budget` pays one unit per
+// row and per point.
+template <bool EXACT>
+__device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p0, int p1, float band, float& best,
+                                          float& second, int& bpos, int& borig, double& bD, int& budget) {
+  budget -= 1 + (p1 - p0);
+  if (budget < 0) return;
+  for (int p = p0; p < p1; ++p) scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
 }
 
 // One lane's walk over the rings of cells around the target's cell c (clamped
@@ -1060,7 +1067,7 @@ __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p
 template <bool EXACT>
 __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, const int (&b0)[3], const int (&b1)[3],
                                            const int (&c)[3], const float (&gc)[3], float band, float& best,
-                                           float& second, int& bpos, int& borig, double& bD) {
+                                           float& second, int& bpos, int& borig, double& bD, int& budget) {
   const GridParams& g = S.g;
   const float h = g.h;
   const float to[3] = {q.tx, q.ty, q.tz}, oo[3] = {g.ox, g.oy, g.oz};
@@ -1092,6 +1099,7 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
       const float gz2 = gz * gz;
       const bool zshell = kz == c[2] - s || kz == c[2] + s;
       for (int jy = y0; jy <= y1; ++jy) {
+        if (budget < 0) return;  // out of budget: the warp searches this sample
         const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
         const float gy = axis_gap(jy, q.ty, g.oy, h);
         const float gyz = fmaf(gy, gy, gz2);
@@ -1108,55 +1116,210 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
           }
           if (x0 <= x1)
             lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + x0), __ldg(S.cell_start + rowbase + x1 + 1), band,
-                             best, second, bpos, borig, bD);
+                             best, second, bpos, borig, bD, budget);
         } else {
           // a row inside the ring's y-z square: only its two end cells are on the ring
           if (has_l && fmaf(gxl, gxl, gyz) <= bound)
             lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + xl), __ldg(S.cell_start + rowbase + xl + 1), band,
-                             best, second, bpos, borig, bD);
+                             best, second, bpos, borig, bD, budget);
           if (has_r && fmaf(gxr, gxr, gyz) <= (EXACT ? bound : best * (1.0f + kRelPrune)))
             lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + xr), __ldg(S.cell_start + rowbase + xr + 1), band,
-                             best, second, bpos, borig, bD);
+                             best, second, bpos, borig, bD, budget);
         }
       }
     }
   }
 }
 
-// Nearest point strictly inside box q, searched by this lane alone: sorted
-// position and original index, or -1 when the box holds no point.
-__device__ __forceinline__ void lane_search(const SnapDev& S, const BoxQ& q, int& pos, int& orig) {
-  const GridParams& g = S.g;
-  pos = -1;
-  orig = -1;
+// The cells of box q: b0..b1 per axis, the target's cell c (clamped into the
+// grid) and the squared gaps from the target to c's faces; false when the box
+// misses the grid.
+__device__ __forceinline__ bool box_cells(const GridParams& g, const BoxQ& q, int (&b0)[3], int (&b1)[3], int (&c)[3],
+                                          float (&gc)[3]) {
   if (!(q.lox < g.maxx && q.hix > g.minx && q.loy < g.maxy && q.hiy > g.miny && q.loz < g.maxz &&
         q.hiz > g.minz && q.lox < q.hix && q.loy < q.hiy && q.loz < q.hiz))
-    return;
-  const int b0[3] = {cell_coord(q.lox, g.ox, g.inv_h, g.dx), cell_coord(q.loy, g.oy, g.inv_h, g.dy),
-                     cell_coord(q.loz, g.oz, g.inv_h, g.dz)};
-  const int b1[3] = {cell_coord(q.hix, g.ox, g.inv_h, g.dx), cell_coord(q.hiy, g.oy, g.inv_h, g.dy),
-                     cell_coord(q.hiz, g.oz, g.inv_h, g.dz)};
-  const int c[3] = {cell_coord(q.tx, g.ox, g.inv_h, g.dx), cell_coord(q.ty, g.oy, g.inv_h, g.dy),
-                    cell_coord(q.tz, g.oz, g.inv_h, g.dz)};
+    return false;
+  b0[0] = cell_coord(q.lox, g.ox, g.inv_h, g.dx);
+  b0[1] = cell_coord(q.loy, g.oy, g.inv_h, g.dy);
+  b0[2] = cell_coord(q.loz, g.oz, g.inv_h, g.dz);
+  b1[0] = cell_coord(q.hix, g.ox, g.inv_h, g.dx);
+  b1[1] = cell_coord(q.hiy, g.oy, g.inv_h, g.dy);
+  b1[2] = cell_coord(q.hiz, g.oz, g.inv_h, g.dz);
+  c[0] = cell_coord(q.tx, g.ox, g.inv_h, g.dx);
+  c[1] = cell_coord(q.ty, g.oy, g.inv_h, g.dy);
+  c[2] = cell_coord(q.tz, g.oz, g.inv_h, g.dz);
   const float gx = axis_gap(c[0], q.tx, g.ox, g.h), gy = axis_gap(c[1], q.ty, g.oy, g.h),
               gz = axis_gap(c[2], q.tz, g.oz, g.h);
-  const float gc[3] = {gx * gx, gy * gy, gz * gz};
+  gc[0] = gx * gx;
+  gc[1] = gy * gy;
+  gc[2] = gz * gz;
+  return true;
+}
+
+constexpr int kLaneBudget = 384;  // rows + points one lane may scan for one sample
+
+// Nearest point strictly inside box q, searched by this lane alone: sorted
+// position and original index, or -1 when the box holds no point.  False when
+// the search ran out of `budget` (dense cells, or a wide box far from the
+// points): a whole warp then searches the sample (warp_search, march_hard).
+__device__ __forceinline__ bool lane_search(const SnapDev& S, const BoxQ& q, int& pos, int& orig, int budget) {
+  pos = -1;
+  orig = -1;
+  int b0[3], b1[3], c[3];
+  float gc[3];
+  if (!box_cells(S.g, q, b0, b1, c, gc)) return true;
   float best = FLT_MAX, second = FLT_MAX;
   int bpos = -1, borig = -1;
   double bD = DBL_MAX;
-  lane_rings<false>(S, q, b0, b1, c, gc, 0.0f, best, second, bpos, borig, bD);
-  if (bpos < 0) return;
+  lane_rings<false>(S, q, b0, b1, c, gc, 0.0f, best, second, bpos, borig, bD, budget);
+  if (budget < 0) return false;
+  if (bpos < 0) return true;
   if (second <= best * (1.0f + kRelTie)) {
     // possible FP64 tie (or an exact FP32 tie): re-rank the contenders
     float fb = FLT_MAX, fs = FLT_MAX;
     int p2 = -1, o2 = 0x7fffffff;
     double D2 = DBL_MAX;
-    lane_rings<true>(S, q, b0, b1, c, gc, best * (1.0f + kRelTie), fb, fs, p2, o2, D2);
+    lane_rings<true>(S, q, b0, b1, c, gc, best * (1.0f + kRelTie), fb, fs, p2, o2, D2, budget);
+    if (budget < 0) return false;
     bpos = p2;
     borig = o2;
   }
   pos = bpos;
   orig = borig;
+  return true;
+}
+
+// Warp-collective walk over the same rings as lane_rings for one sample (q
+// the same in every lane): the rows of a ring are spread over the lanes, their
+// point ranges prefix-summed and loaded 32 per round.  Each lane keeps the
+// best of the points it scanned; the pruning bound is the warp's best, taken
+// after every ring.
+template <bool EXACT>
+__device__ __forceinline__ void warp_rings(const SnapDev& S, const BoxQ& q, const int (&b0)[3], const int (&b1)[3],
+                                           const int (&c)[3], const float (&gc)[3], float band, float& best,
+                                           float& second, int& bpos, int& borig, double& bD) {
+  const GridParams& g = S.g;
+  const float h = g.h;
+  const int lane = threadIdx.x & 31;
+  const float to[3] = {q.tx, q.ty, q.tz}, oo[3] = {g.ox, g.oy, g.oz};
+  float bound = EXACT ? band * (1.0f + kRelPrune) : FLT_MAX;
+  for (int s = 0;; ++s) {
+    if (c[0] - s < b0[0] && c[0] + s > b1[0] && c[1] - s < b0[1] && c[1] + s > b1[1] && c[2] - s < b0[2] &&
+        c[2] + s > b1[2])
+      break;  // no cell of this ring lies in the box
+    if (s >= 1) {
+      float lb2 = FLT_MAX;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        float m = FLT_MAX;
+        if (c[j] - s >= b0[j]) m = axis_gap(c[j] - s, to[j], oo[j], h);
+        if (c[j] + s <= b1[j]) m = fminf(m, axis_gap(c[j] + s, to[j], oo[j], h));
+        if (m < FLT_MAX) lb2 = fminf(lb2, fmaf(m, m, gc[(j + 1) % 3] + gc[(j + 2) % 3]));
+      }
+      if (lb2 > bound) break;
+    }
+    const int xl = c[0] - s, xr = c[0] + s;
+    const bool has_l = xl >= b0[0], has_r = s > 0 && xr <= b1[0];
+    const float gxl = has_l ? axis_gap(xl, q.tx, g.ox, h) : 0.0f;
+    const float gxr = has_r ? axis_gap(xr, q.tx, g.ox, h) : 0.0f;
+    const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
+    const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
+    const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
+    for (int rb = 0; rb < nrows; rb += 32) {
+      // this lane's row of the ring: up to two point ranges
+      const int rr = rb + lane;
+      int a0 = 0, n0 = 0, a1 = 0, n1 = 0;
+      if (rr < nrows) {
+        const int jy = y0 + rr % nyr, kz = z0 + rr / nyr;
+        const float gz = axis_gap(kz, q.tz, g.oz, h);
+        const float gy = axis_gap(jy, q.ty, g.oy, h);
+        const float gyz = fmaf(gy, gy, gz * gz);
+        if (gyz + gc[0] <= bound) {
+          const int rowbase = (kz * g.dy + jy) * g.dx;
+          if (kz == c[2] - s || kz == c[2] + s || jy == c[1] - s || jy == c[1] + s) {
+            int x0 = max(xl, b0[0]), x1 = min(xr, b1[0]);
+            if (bound < FLT_MAX) {
+              const float rem = fmaxf(bound - gyz, 0.0f);
+              const float rx = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
+              x0 = max(x0, cell_coord(q.tx - rx, g.ox, g.inv_h, g.dx));
+              x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
+            }
+            if (x0 <= x1) {
+              a0 = __ldg(S.cell_start + rowbase + x0);
+              n0 = __ldg(S.cell_start + rowbase + x1 + 1) - a0;
+            }
+          } else {
+            if (has_l && fmaf(gxl, gxl, gyz) <= bound) {
+              a0 = __ldg(S.cell_start + rowbase + xl);
+              n0 = __ldg(S.cell_start + rowbase + xl + 1) - a0;
+            }
+            if (has_r && fmaf(gxr, gxr, gyz) <= bound) {
+              a1 = __ldg(S.cell_start + rowbase + xr);
+              n1 = __ldg(S.cell_start + rowbase + xr + 1) - a1;
+            }
+          }
+        }
+      }
+      const int n = n0 + n1;
+      const int incl = warp_incl_scan(n);
+      const int excl = incl - n;
+      const int total = __shfl_sync(kFull, incl, 31);
+      for (int ib = 0; ib < total; ib += 32) {
+        const int i = ib + lane;
+        const int own = warp_owner(incl, i) & 31;
+        const int oa0 = __shfl_sync(kFull, a0, own), on0 = __shfl_sync(kFull, n0, own);
+        const int oa1 = __shfl_sync(kFull, a1, own), oe = __shfl_sync(kFull, excl, own);
+        if (i < total) {
+          const int k = i - oe;
+          const int p = k < on0 ? oa0 + k : oa1 + (k - on0);
+          scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
+        }
+      }
+    }
+    if (!EXACT) bound = warp_min(best) * (1.0f + kRelPrune);
+  }
+}
+
+// Warp-collective: nearest point strictly inside box q (the same q in every
+// lane), the same result as lane_search; every lane gets it.
+__device__ __noinline__ void warp_search(const SnapDev& S, const BoxQ& q, int& pos, int& orig) {
+  const int lane = threadIdx.x & 31;
+  pos = -1;
+  orig = -1;
+  int b0[3], b1[3], c[3];
+  float gc[3];
+  if (!box_cells(S.g, q, b0, b1, c, gc)) return;
+  float best = FLT_MAX, second = FLT_MAX;
+  int bpos = -1, borig = -1;
+  double bD = DBL_MAX;
+  warp_rings<false>(S, q, b0, b1, c, gc, 0.0f, best, second, bpos, borig, bD);
+  const float b1v = warp_min(best);
+  if (b1v == FLT_MAX) return;  // no point in the box
+  // the lowest lane holding the best, and the warp's second best
+  const int hl = __ffs(__ballot_sync(kFull, best == b1v)) - 1;
+  const float sec = warp_min(lane == hl ? second : best);
+  int P = __shfl_sync(kFull, bpos, hl), O = __shfl_sync(kFull, borig, hl);
+  if (sec <= b1v * (1.0f + kRelTie)) {
+    // possible FP64 tie: the exact re-rank, reduced over the warp by (distance, original index)
+    float fb = FLT_MAX, fs = FLT_MAX;
+    int p2 = -1, o2 = 0x7fffffff;
+    double D2 = DBL_MAX;
+    warp_rings<true>(S, q, b0, b1, c, gc, b1v * (1.0f + kRelTie), fb, fs, p2, o2, D2);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const double Do = __shfl_xor_sync(kFull, D2, off);
+      const int oo = __shfl_xor_sync(kFull, o2, off), po = __shfl_xor_sync(kFull, p2, off);
+      if (Do < D2 || (Do == D2 && oo < o2)) {
+        D2 = Do;
+        o2 = oo;
+        p2 = po;
+      }
+    }
+    P = p2;
+    O = o2;
+  }
+  pos = P;
+  orig = O;
 }
 
 // Ray context of lane `src` (every lane takes part).
@@ -1237,6 +1400,22 @@ __device__ __forceinline__ void add_emission(const MarchArgs& a, const RayCtx& r
 // from the front of the buffer, then the overflow records from the back.
 __device__ __forceinline__ DeferredRec deferred_at(const MarchArgs& a, int64_t nfront, int64_t ri) {
   return ri < nfront ? a.deferred[ri] : a.deferred[a.deferred_cap - 1 - (ri - nfront)];
+}
+
+// A deferred sample's result: its NN index, and its neighbour and LOS speed
+// staged for the emission step.
+__device__ __forceinline__ void store_deferred(const MarchArgs& a, const RayCtx& r, int k, int kind, int p, int o,
+                                               int* sp, float* sv) {
+  const ViewDesc* V = a.views + r.v;
+  int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+  if (nnout) nnout[((int64_t)r.i * V->nx + r.j) * V->nz + k] = o;
+  float vl = 0.0f;
+  if (p >= 0 && kind == kDeferredSpectral) {
+    const float4 vv = __ldg(a.snap.vel + p);
+    vl = fmaf(V->uz, vv.z, fmaf(V->uy, vv.y, V->ux * vv.x));
+  }
+  *sp = p;
+  *sv = vl;
 }
 
 // ---------------------------------------------------------------------------
@@ -1344,6 +1523,9 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
       const int r1 = r0 + max(__popc(fits), 1);
       const int nsamp = __shfl_sync(kFull, incl, r1 - 1) - start;
       // 1. one sample per lane: its record, ray and box, then its own search
+      // within a budget; a sample that exceeds it goes to the hard queue
+      // (searched by a whole warp in march_hard) and adds nothing here
+      const int budget = a.hard_cap > 0 ? kLaneBudget : 0x7fffffff;
       for (int t0 = 0; t0 < nsamp; t0 += 32) {
         const int t = t0 + lane;
         const int own = warp_owner(incl, start + t) & 31;  // the record lane holding flattened sample t
@@ -1351,21 +1533,37 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
         const unsigned oz = __shfl_sync(kFull, rec.z, own), ow = __shfl_sync(kFull, rec.w, own);
         const int oe = __shfl_sync(kFull, excl, own);
         const RayCtx r = shfl_ray(mine, own);
+        bool hard = false;
+        int k = 0, p = -1, o = -1;
+        BoxQ q{};
         if (t < nsamp) {
-          const int k = (int)oy + nth_set_bit(oz, ow, start + t - oe);
-          int p, o;
-          lane_search(a.snap, exact_box(r, k), p, o);
-          const ViewDesc* V = a.views + r.v;
-          int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
-          if (nnout) nnout[((int64_t)r.i * V->nx + r.j) * V->nz + k] = o;
-          float vl = 0.0f;
-          if (p >= 0 && kind == kDeferredSpectral) {
-            const float4 vv = __ldg(a.snap.vel + p);
-            vl = fmaf(V->uz, vv.z, fmaf(V->uy, vv.y, V->ux * vv.x));
-          }
-          spos[w][t] = p;
-          svlos[w][t] = vl;
+          k = (int)oy + nth_set_bit(oz, ow, start + t - oe);
+          q = exact_box(r, k);
+          hard = !lane_search(a.snap, q, p, o, budget);
         }
+        const unsigned hm = __ballot_sync(kFull, hard);
+        unsigned long long hb = 0;
+        if (hm && lane == 0) hb = atomicAdd(a.counter + kCtrHard, (unsigned long long)__popc(hm));
+        hb = __shfl_sync(kFull, hb, 0);
+        if (hard) {
+          const int64_t slot = (int64_t)hb + __popc(hm & ((1u << lane) - 1u));
+          if (slot < a.hard_cap) {
+            a.hard[slot] = make_uint2(r.item, (unsigned)k);
+            p = -1;  // its neighbour and emission come from march_hard
+          } else {
+            lane_search(a.snap, q, p, o, 0x7fffffff);  // queue full: finish here
+            hard = false;
+          }
+        }
+        if (t < nsamp) {
+          if (hard) {
+            spos[w][t] = -1;
+            svlos[w][t] = 0.0f;
+          } else {
+            store_deferred(a, r, k, kind, p, o, spos[w] + t, svlos[w] + t);
+          }
+        }
+        if (a.stats && hm && lane == 0) atomicAdd(a.stats + kStatHard, (unsigned long long)__popc(hm));
       }
       __syncwarp();
       // 2. their emission, record by record
@@ -1378,6 +1576,37 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
       __syncwarp();  // the staging arrays are rewritten by the next batch
       r0 = r1;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Hard samples: deferred samples whose one-lane search ran out of budget
+// (dense cells, or a wide box reaching far from the points).  One warp per
+// sample, from a queue shared by the whole grid: the rows and points of each
+// ring are spread over the lanes (warp_search).  The warp writes the NN index
+// and adds the sample's emission with atomics.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, kMinCtas) march_hard(MarchArgs a, const double3* __restrict__ ktab,
+                                                       int ktab_stride, int kind) {
+  __shared__ int sp[kWarps];
+  __shared__ float sv[kWarps];
+  const int w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t n = min((int64_t)a.counter[kCtrHard], a.hard_cap);  // written by march_deferred
+  for (;;) {
+    unsigned long long i = 0;
+    if (lane == 0) i = atomicAdd(a.counter + kCtrHardHead, 1ull);
+    i = __shfl_sync(kFull, i, 0);
+    if ((int64_t)i >= n) return;
+    const uint2 hs = a.hard[i];
+    RayCtx r;
+    if (!ray_of_item(a, ktab, ktab_stride, (int64_t)hs.x, r)) continue;  // queued from real rays only
+    int p, o;
+    warp_search(a.snap, exact_box(r, (int)hs.y), p, o);
+    if (lane == 0) store_deferred(a, r, (int)hs.y, kind, p, o, sp + w, sv + w);
+    __syncwarp();
+    if (p >= 0) add_emission(a, r, kind, sp + w, sv + w, 1);
+    __syncwarp();  // sp / sv are rewritten by the next sample
   }
 }
 
@@ -1406,6 +1635,16 @@ cudaError_t launch_deferred(const MarchArgs& a, const double3* ktab, int ktab_st
   // the record count is known on the device only: a persistent grid that
   // drains the queue (and exits at once when it is empty)
   march_deferred<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hard(const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count, cudaStream_t s,
+                        int kind) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_hard, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  march_hard<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
   return cudaGetLastError();
 }
 
@@ -1462,8 +1701,9 @@ cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_strid
   if (e != cudaSuccess) return e;
   const int kind = a.s2 ? kDeferredThomson : (imaging ? kDeferredImaging : kDeferredSpectral);
   e = launch_split(a, ktab, ktab_stride, sm_count, s, kind);
-  if (e != cudaSuccess) return e;
-  return launch_deferred(a, ktab, ktab_stride, sm_count, s, kind);
+  if (e == cudaSuccess) e = launch_deferred(a, ktab, ktab_stride, sm_count, s, kind);
+  if (e != cudaSuccess || a.hard_cap <= 0) return e;
+  return launch_hard(a, ktab, ktab_stride, sm_count, s, kind);
 }
 
 }  // namespace fomo

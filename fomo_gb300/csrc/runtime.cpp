@@ -725,6 +725,8 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     }
     G.deferred_cap = deferred_capacity(items, G.maxnz);
     G.o_def = L.take(sizeof(DeferredRec) * (size_t)G.deferred_cap);
+    G.hard_cap = hard_capacity(items, G.maxnz);
+    G.o_hard = L.take(sizeof(uint2) * (size_t)G.hard_cap);
     G.o_s2 = G.method == FOMO_METHOD_THOMSON ? L.take(sizeof(float) * (size_t)G.nv * snap.n) : 0;
   }
   plan->dev_bytes = L.off;
@@ -873,6 +875,8 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.counter = reinterpret_cast<unsigned long long*>(db + G.o_ctr);
     a.deferred = reinterpret_cast<DeferredRec*>(db + G.o_def);
     a.deferred_cap = G.deferred_cap;
+    a.hard = reinterpret_cast<uint2*>(db + G.o_hard);
+    a.hard_cap = G.hard_cap;
     a.nn_idx = G.any_nn ? reinterpret_cast<int32_t* const*>(db + G.o_nnp) : nullptr;
     a.s2 = s2;
     a.totpol = G.totpol;
@@ -1016,11 +1020,11 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
     cudaMemcpy(h, ctx->march_stats, sizeof(h), cudaMemcpyDeviceToHost);
     std::fprintf(stderr,
                  "fomo march stats: segments %llu candidates %llu rows %llu points_loaded %llu not_gathered %llu "
-                 "fallbacks %llu (ambiguous %llu no_candidate %llu far %llu union %llu records %llu) samples %llu "
-                 "scanned %llu ties %llu\n",
+                 "fallbacks %llu (ambiguous %llu no_candidate %llu far %llu deferred %llu records %llu hard %llu) "
+                 "samples %llu scanned %llu ties %llu\n",
                  h[kStatSegments], h[kStatCandidates], h[kStatRows], h[kStatPointsLoaded], h[kStatNotGathered],
                  h[kStatFallbacks], h[kStatFbAmb], h[kStatFbNoCand], h[kStatFbFar], h[kStatFbUnion],
-                 h[kStatDeferredRecs], h[kStatSamples], h[kStatScanned], h[kStatTies]);
+                 h[kStatDeferredRecs], h[kStatHard], h[kStatSamples], h[kStatScanned], h[kStatTies]);
     cudaFree(ctx->march_stats);
   }
   ctx->scratch.release();

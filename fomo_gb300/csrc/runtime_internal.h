@@ -99,6 +99,8 @@ struct PlanGroup {
   size_t o_def = 0;          // deferred-sample records
   std::vector<std::pair<float*, size_t>> zero_outs;  // projection outputs to clear before the scatter
   int64_t deferred_cap = 0;  // records: one per segment of every work item
+  size_t o_hard = 0;
+  int64_t hard_cap = 0;      // hard-sample queue entries
   std::vector<int64_t> item_off;  // first work item of each view (nv + 1 entries)
   std::vector<double> vcost;      // LOS samples + output cells of each view
   size_t out_bytes = 0;           // cube bytes of all its requests

@@ -89,10 +89,11 @@ struct fomo_server {
 namespace {
 
 size_t request_cost(const fomo_request& q) {
-  // output cube + per-view descriptors and tables (generous) + the deferred-sample queue
+  // output cube + per-view descriptors and tables (generous) + the deferred-sample and hard-sample queues
   const size_t rays = (size_t)(q.nx + 31) * (size_t)(q.ny + 31);  // tile padding included
   return cube_elems(q) * sizeof(float) + (size_t)q.nz * 24 + (size_t)(q.nx + q.ny) * 8 + 64 * 1024 +
-         rays * (size_t)((q.nz + 63) / 64) * sizeof(DeferredRec);
+         rays * (size_t)((q.nz + 63) / 64) * sizeof(DeferredRec) +
+         (size_t)hard_capacity((int64_t)rays, q.nz) * sizeof(uint2);
 }
 
 void finish_slot(fomo_server* S, Slot& sl, int status) {

@@ -83,3 +83,22 @@ def test_thomson_off_equator_full_size_sampled_rows(ctx):
         _, oi, _ = oracle.thomson_render(ts, tot, pol, l, b, 256, 256, 1024, rows=(r0, r0 + 1), want_idx=True)
         np.testing.assert_array_equal(idx[r0:r0 + 1], oi)
     ctx.drop_snapshot(sid)
+
+
+def test_wide_boxes_dense_cells_full_cube(ctx):
+    """A 524,288-point flux rope at 64 x 64 pixels and 256 LOS samples: boxes
+    about 1 Mm wide and rope cells of ~90 points, where one lane's ring search
+    runs out of budget and whole warps search those samples (march_hard).
+    Every sample's neighbour index equal to the oracle's, the cube within 1e-4."""
+    s = synth.flux_rope_snapshot(512 * 1024, seed=20)
+    t = synth.line_table()
+    sid, tid = ctx.snapshot(s), ctx.table(t)
+    eps, w = oracle.emission(s, t)
+    width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+    for (l, b) in ((0.5, 0.2), (1.2, -0.3)):
+        cube, idx, _ = ctx.render(ctx.request(sid, tid, fg.METHOD_NN, 64, 64, 256, 16, l, b, width), want_idx=True)
+        oc, oi, _ = oracle.nn_render(s, eps, w, t.lambda0, l, b, 64, 64, 256, 16, width, want_idx=True)
+        np.testing.assert_array_equal(idx, oi)
+        assert G.norm_max_err(cube.ravel(), oc.ravel()) <= TOL
+    ctx.drop_snapshot(sid)
+
