@@ -609,7 +609,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
       const float inv_dy = fabsf(sdy) > 1e-30f ? 1.0f / sdy : 0.0f;
       const float inv_dz = fabsf(sdz) > 1e-30f ? 1.0f / sdz : 0.0f;
       const unsigned lt = (1u << lane) - 1u;
-      for (int rb = 0; rb < nrows; rb += 32) {
+      for (int rb = 0; rb < nrows && count <= kSegCap; rb += 32) {
         const int rr = rb + lane;
         int n = 0, base = 0;
         if (rr < nrows) {
@@ -1156,7 +1156,7 @@ __device__ __forceinline__ bool box_cells(const GridParams& g, const BoxQ& q, in
   return true;
 }
 
-constexpr int kLaneBudget = 384;  // rows + points one lane may scan for one sample
+constexpr int kLaneBudget = 192;  // rows + points one lane may scan for one sample
 
 // Nearest point strictly inside box q, searched by this lane alone: sorted
 // position and original index, or -1 when the box holds no point.  False when
@@ -1500,14 +1500,18 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
   // (at most one record per segment)
   const int64_t nfront = min((int64_t)a.counter[kCtrDeferred], a.deferred_cap);
   const int64_t nrec = nfront + min((int64_t)a.counter[kCtrOverflow], a.deferred_cap - nfront);
+  // records per grab: 32, or fewer when the queue is short, so that every
+  // warp of the grid gets a share (a small render has few records)
+  const int64_t nwarps = (int64_t)gridDim.x * kWarps;
+  const int grab = (int)max((int64_t)1, min((int64_t)32, nrec / nwarps));
   for (;;) {
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(a.counter + kCtrDeferredHead, 32ull);
+    if (lane == 0) base = atomicAdd(a.counter + kCtrDeferredHead, (unsigned long long)grab);
     base = __shfl_sync(kFull, base, 0);
     if ((int64_t)base >= nrec) return;
     const int64_t ri = (int64_t)base + lane;
     DeferredRec rec = make_uint4(0u, 0u, 0u, 0u);
-    if (ri < nrec) rec = deferred_at(a, nfront, ri);
+    if (lane < grab && ri < nrec) rec = deferred_at(a, nfront, ri);
     const int cnt = __popc(rec.z) + __popc(rec.w);
     const int incl = warp_incl_scan(cnt);
     const int excl = incl - cnt;
