@@ -1051,11 +1051,13 @@ __device__ __forceinline__ void scan_point(const float4 v, int p, const BoxQ& q,
 }
 
 // Candidates p in [p0, p1), one after the other; `budget` pays one unit per
-// row and per point.
+// row and per point.  A range of more than kLaneDense points (dense cells)
+// spends the whole budget at once: such samples are searched by a warp.
+constexpr int kLaneDense = 48;
 template <bool EXACT>
 __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p0, int p1, float band, float& best,
                                           float& second, int& bpos, int& borig, double& bD, int& budget) {
-  budget -= 1 + (p1 - p0);
+  budget -= (p1 - p0 > kLaneDense && budget < 0x3fffffff) ? 0x3fffffff : 1 + (p1 - p0);
   if (budget < 0) return;
   for (int p = p0; p < p1; ++p) scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
 }
