@@ -428,11 +428,13 @@ def run_ours(args):
                          "bytes_per_sample": bps,
                          "kernel": "march_spectral<4,1> (first search pass + emission sums) + march_split "
                                    "(overflowing segments) + march_deferred (the samples the first pass "
-                                   "leaves), timed together"},
+                                   "leaves) + march_hard (deferred samples over the one-lane budget), "
+                                   "timed together"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            # per step: view init, view extents, view finalize, first-pass march, overflow split, deferred march
-            "gpu_launches": 6 * args.steps,
+            # per step: view init, view extents, view finalize, first-pass march, overflow split, deferred march,
+            # hard-sample march
+            "gpu_launches": 7 * args.steps,
             "serving": serving,
         }
         print(json.dumps(out))
