@@ -646,6 +646,16 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
       plan->groups[it->second].reqs.push_back(r);
     }
   }
+  // launches with less work first (a server completes their requests sooner)
+  {
+    auto work = [&](const PlanGroup& G) {
+      double w = 0.0;
+      for (int r : G.reqs) w += (double)reqs[r].nx * reqs[r].ny * reqs[r].nz;
+      return w;
+    };
+    std::stable_sort(plan->groups.begin(), plan->groups.end(),
+                     [&](const PlanGroup& a, const PlanGroup& b) { return work(a) < work(b); });
+  }
   Layout L;
   const size_t hdr = L.take(0);
   (void)hdr;
@@ -824,7 +834,21 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
 // Cut points [0 = c0 < c1 < ... = nv] of the view ranges a launch marches in
 // when its cubes download as they complete: about equal shares of the views'
 // cost, one range per 256 MB of cubes, 8 at most.
-static std::vector<int> view_ranges(const PlanGroup& G, bool split) {
+static std::vector<int> view_ranges(const PlanGroup& G, bool split, double range_cost) {
+  if (split && range_cost > 0.0) {
+    // ranges of about range_cost each (views in plan order: smaller images first)
+    std::vector<int> cuts{0};
+    double acc = 0.0;
+    for (int v = 0; v < G.nv; ++v) {
+      if (v > cuts.back() && acc >= range_cost) {
+        cuts.push_back(v);
+        acc = 0.0;
+      }
+      acc += G.vcost[v];
+    }
+    cuts.push_back(G.nv);
+    return cuts;
+  }
   const size_t n = split ? std::min<size_t>({8, (size_t)G.nv, std::max<size_t>(1, G.out_bytes >> 28)}) : 1;
   double total = 0.0;
   for (double c : G.vcost) total += c;
@@ -838,7 +862,8 @@ static std::vector<int> view_ranges(const PlanGroup& G, bool split) {
   return cuts;
 }
 
-int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done) {
+int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done,
+               double range_cost) {
   char* db = scr->arena.base;
   // Under stream capture an ordinary event record is only a capture-internal
   // dependency: the staging event is then recorded after the graph launch,
@@ -891,7 +916,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     } else if (e == cudaSuccess) {
       // the march over view ranges: each range's rays are a contiguous run of
       // work items, with the work counters cleared before it
-      const std::vector<int> cuts = view_ranges(G, done != nullptr);
+      const std::vector<int> cuts = view_ranges(G, done != nullptr, range_cost);
       for (size_t k = 0; k + 1 < cuts.size() && e == cudaSuccess && rc == FOMO_OK; ++k) {
         if (k > 0) e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * kCtrCount, s);
         a.item_base = G.item_off[cuts[k]];

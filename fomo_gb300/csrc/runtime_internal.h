@@ -171,14 +171,17 @@ int validate(fomo_ctx* ctx, const fomo_request& q);
 size_t cube_elems(const fomo_request& q);
 // Called by issue_plan once the work of views [v0, v1) of launch G is on the
 // stream: their cubes are complete when the stream reaches that point.  With
-// it, a large launch marches in up to 8 view ranges (one per 256 MB of cubes).
+// it, a launch marches in view ranges: ranges of about `range_cost` LOS
+// samples + output cells each when that is > 0, else up to 8 ranges, one per
+// 256 MB of cubes.
 using RangeDone = std::function<int(const PlanGroup& G, int v0, int v1)>;
 int enqueue_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
                   cudaStream_t s, std::vector<ViewDesc>* views_out, std::vector<int>* view_of_req,
                   const RangeDone* done = nullptr);
 int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
                ScratchSet* scr, Plan* plan);
-int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done = nullptr);
+int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done = nullptr,
+               double range_cost = 0.0);
 std::string workload_class(const PlanGroup& G, const SnapRec& snap);
 int order_streams(fomo_ctx* ctx, cudaStream_t s);
 SnapDev snap_dev(const SnapRec& r);

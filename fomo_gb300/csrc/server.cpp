@@ -8,8 +8,12 @@
 // group, shared neighbour lookups for requests with the same view) and
 // enqueues it on the slot's stream.  While one slot's batch runs, requests
 // that arrive meanwhile are admitted into the other slot, so their work
-// overlaps on the device.  Results go device -> pinned staging -> the
-// caller's buffer; each request records submit / admit / start / done times.
+// overlaps on the device.  A slot's batch marches in view ranges of bounded
+// work, launches with less work first and smaller images first within a
+// launch; each range's cubes download as soon as it is done and its requests
+// complete then, without waiting for the rest of the batch.  Results go
+// device -> pinned staging -> the caller's buffer; each request records
+// submit / admit / start / done times.
 //
 // A request is rendered by the same kernels, with the same per-ray work, as
 // when it is rendered alone: one warp owns one ray and nothing in a ray's
@@ -61,9 +65,18 @@ struct Slot {
   char* pinned = nullptr; // host staging of the cubes
   size_t pinned_cap = 0;
   std::vector<uint64_t> ids;
+  size_t cost = 0;        // admission bytes of the batch
+  // view ranges of the batch in issue order: the event after each range's
+  // downloads, and its requests
+  std::vector<cudaEvent_t> evpool;
+  std::deque<std::pair<cudaEvent_t, std::vector<uint64_t>>> ranges;
   bool busy = false;
   double t_launch = 0;
 };
+
+// Work per view range of a slot's batch (LOS samples + output cells): about a
+// millisecond of march.
+constexpr double kServeRangeCost = double(1 << 24);
 
 }  // namespace
 
@@ -96,22 +109,32 @@ size_t request_cost(const fomo_request& q) {
          (size_t)hard_capacity((int64_t)rays, q.nz) * sizeof(uint2);
 }
 
-void finish_slot(fomo_server* S, Slot& sl, int status) {
-  // called with S->mu held
+// Requests `ids` of slot sl are complete (their cubes are in pinned staging);
+// called with S->mu held.
+void finish_ids(fomo_server* S, Slot& sl, const std::vector<uint64_t>& ids, int status) {
   const double t = now_s() - S->t0;
-  for (uint64_t id : sl.ids) {
+  for (uint64_t id : ids) {
     auto it = S->tickets.find(id);
     if (it == S->tickets.end()) continue;
     Ticket& T = it->second;
+    if (T.state == TState::kDone) continue;
     if (status == FOMO_OK && !T.cancelled && T.out_host)
       std::memcpy(T.out_host, sl.pinned + T.host_off, T.out_bytes);
     T.status = T.cancelled ? FOMO_ECANCELLED : status;
     T.state = TState::kDone;
     T.t_done = t;
-    S->inflight_bytes -= T.cost;
-    S->inflight -= 1;
   }
+}
+
+// The whole batch of slot sl is done: its remaining requests complete and its
+// memory counts as free for admission; called with S->mu held.
+void finish_slot(fomo_server* S, Slot& sl, int status) {
+  finish_ids(S, sl, sl.ids, status);
+  S->inflight_bytes -= sl.cost;
+  S->inflight -= (int)sl.ids.size();
   sl.ids.clear();
+  sl.ranges.clear();
+  sl.cost = 0;
   sl.busy = false;
 }
 
@@ -143,14 +166,34 @@ int launch_slot(fomo_server* S, Slot& sl, std::vector<uint64_t>& ids, std::vecto
   if (rc) return rc;
   rc = order_streams(ctx, sl.stream);
   if (rc) return rc;
-  rc = issue_plan(ctx, plan, &sl.scr, sl.stream);
+  // each view range: download its cubes, then an event that completes its requests
+  std::deque<std::pair<cudaEvent_t, std::vector<uint64_t>>> ranges;
+  size_t nev = 0;
+  RangeDone done = [&](const PlanGroup& G, int v0, int v1) -> int {
+    std::vector<uint64_t> rids;
+    for (int v = v0; v < v1; ++v)
+      for (int i : G.vreqs[v]) {
+        cudaError_t e = cudaMemcpyAsync(sl.pinned + doff[i], d[i], out_bytes[i], cudaMemcpyDeviceToHost, sl.stream);
+        if (e != cudaSuccess) return cuda_err(ctx, e, "result download");
+        rids.push_back(ids[i]);
+      }
+    if (nev == sl.evpool.size()) {
+      cudaEvent_t ev = nullptr;
+      cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_err(ctx, e, "range event");
+      sl.evpool.push_back(ev);
+    }
+    const cudaEvent_t ev = sl.evpool[nev++];
+    cudaError_t e = cudaEventRecord(ev, sl.stream);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "range event");
+    ranges.emplace_back(ev, std::move(rids));
+    return FOMO_OK;
+  };
+  rc = issue_plan(ctx, plan, &sl.scr, sl.stream, &done, kServeRangeCost);
   if (rc) return rc;
-  for (int i = 0; i < n; ++i) {
-    cudaError_t e = cudaMemcpyAsync(sl.pinned + doff[i], d[i], out_bytes[i], cudaMemcpyDeviceToHost, sl.stream);
-    if (e != cudaSuccess) return cuda_err(ctx, e, "result download");
-  }
   cudaError_t e = cudaEventRecord(sl.done, sl.stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "slot event");
+  sl.ranges = std::move(ranges);  // only the scheduler thread (this one) reads them
   std::lock_guard<std::mutex> lk(S->mu);
   for (int i = 0; i < n; ++i) {
     auto it = S->tickets.find(ids[i]);
@@ -163,9 +206,19 @@ void scheduler(fomo_server* S) {
   cudaSetDevice(S->ctx->device);
   for (;;) {
     std::unique_lock<std::mutex> lk(S->mu);
-    // completions
+    // completions: view ranges in issue order, then the whole batch
     for (Slot& sl : S->slots) {
       if (!sl.busy) continue;
+      bool any = false;
+      while (!sl.ranges.empty()) {
+        const cudaError_t qr = cudaEventQuery(sl.ranges.front().first);
+        if (qr == cudaErrorNotReady) break;
+        if (qr != cudaSuccess) break;  // a device error: reported with the batch below
+        finish_ids(S, sl, sl.ranges.front().second, FOMO_OK);
+        sl.ranges.pop_front();
+        any = true;
+      }
+      if (any) S->done_cv.notify_all();
       cudaError_t q = cudaEventQuery(sl.done);
       if (q == cudaSuccess) {
         finish_slot(S, sl, FOMO_OK);
@@ -203,6 +256,7 @@ void scheduler(fomo_server* S) {
         T.t_start = t;
         S->inflight_bytes += T.cost;
         S->inflight += 1;
+        free_slot->cost += T.cost;
         ids.push_back(id);
         reqs.push_back(T.req);
         out_bytes.push_back(T.out_bytes);
@@ -212,6 +266,7 @@ void scheduler(fomo_server* S) {
         free_slot->ids = ids;
         lk.unlock();
         int rc = launch_slot(S, *free_slot, ids, reqs, out_bytes);
+        if (rc != FOMO_OK) cudaStreamSynchronize(free_slot->stream);  // part of the batch may be queued
         lk.lock();
         if (rc != FOMO_OK) {
           S->err = S->ctx->err;
@@ -339,6 +394,7 @@ int fomo_server_destroy(fomo_server* S) {
     dev_free(S->ctx, sl.out.base);
     sl.scr.release();
     if (sl.pinned) cudaFreeHost(sl.pinned);
+    for (cudaEvent_t ev : sl.evpool) cudaEventDestroy(ev);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
