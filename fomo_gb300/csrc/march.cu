@@ -1054,10 +1054,11 @@ __device__ __forceinline__ void scan_point(const float4 v, int p, const BoxQ& q,
 // row and per point.  A range of more than kLaneDense points (dense cells)
 // spends the whole budget at once: such samples are searched by a warp.
 constexpr int kLaneDense = 48;
+constexpr int kLaneDenseOnly = 0x3ffffffe;  // budget that only a dense range exhausts
 template <bool EXACT>
 __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p0, int p1, float band, float& best,
                                           float& second, int& bpos, int& borig, double& bD, int& budget) {
-  budget -= (p1 - p0 > kLaneDense && budget < 0x3fffffff) ? 0x3fffffff : 1 + (p1 - p0);
+  budget -= (p1 - p0 > kLaneDense && budget <= kLaneDenseOnly) ? 0x3fffffff : 1 + (p1 - p0);
   if (budget < 0) return;
   for (int p = p0; p < p1; ++p) scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
 }
@@ -1506,6 +1507,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
   // warp of the grid gets a share (a small render has few records)
   const int64_t nwarps = (int64_t)gridDim.x * kWarps;
   const int grab = (int)max((int64_t)1, min((int64_t)32, nrec / nwarps));
+  const bool short_queue = nrec < 32 * nwarps;
   for (;;) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(a.counter + kCtrDeferredHead, (unsigned long long)grab);
@@ -1528,10 +1530,12 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
       const unsigned fits = __ballot_sync(kFull, lane >= r0 && incl - start <= kDefBatch);
       const int r1 = r0 + max(__popc(fits), 1);
       const int nsamp = __shfl_sync(kFull, incl, r1 - 1) - start;
-      // 1. one sample per lane: its record, ray and box, then its own search
-      // within a budget; a sample that exceeds it goes to the hard queue
-      // (searched by a whole warp in march_hard) and adds nothing here
-      const int budget = a.hard_cap > 0 ? kLaneBudget : 0x7fffffff;
+      // 1. one sample per lane: its record, ray and box, then its own search.
+      // A sample in dense cells, or (when the queue is short and latency
+      // matters) one over the budget, goes to the hard queue (a whole warp
+      // searches it in march_hard) and adds nothing here; with a long queue,
+      // 32 lanes on 32 samples keep more loads in flight than a warp on one.
+      const int budget = a.hard_cap <= 0 ? 0x7fffffff : (short_queue ? kLaneBudget : kLaneDenseOnly);
       for (int t0 = 0; t0 < nsamp; t0 += 32) {
         const int t = t0 + lane;
         const int own = warp_owner(incl, start + t) & 31;  // the record lane holding flattened sample t

@@ -47,3 +47,29 @@ def test_noalloc_render_matches_regular_render_on_consecutive_calls():
         rc = lib.fomo_render_noalloc(ctx.h, ctypes.byref(big), ctypes.c_void_p(out.data_ptr()), None)
         assert rc == fg.EINVAL
         assert "limits" in lib.fomo_last_error(ctx.h).decode()
+
+
+def test_noalloc_one_lane_searches_match_warp_searches_on_dense_cells():
+    """The no-allocation path has no hard-sample queue: every deferred sample is
+    searched by one lane without a budget.  On a flux rope at 64 x 64 pixels
+    (wide boxes, ~90-point cells) the regular render sends many samples to
+    whole-warp searches instead; both must find the same neighbours, so the
+    cubes differ only by the order of the deferred passes' atomic additions."""
+    import torch
+
+    with fg.Context(0) as ctx:
+        lib = fg.lib()
+        s = synth.flux_rope_snapshot(512 * 1024, seed=20)
+        t = synth.line_table()
+        sid = ctx.snapshot(s)
+        tid = ctx.table(t)
+        width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+        for (l, b) in ((0.5, 0.2), (1.2, -0.3)):
+            req = ctx.request(sid, tid, fg.METHOD_NN, 64, 64, 256, 16, l, b, width)
+            ref, _, _ = ctx.render(req)
+            out = torch.empty(ref.shape, dtype=torch.float32, device="cuda:0")
+            torch.cuda.synchronize()
+            rc = lib.fomo_render_noalloc(ctx.h, ctypes.byref(req), ctypes.c_void_p(out.data_ptr()), None)
+            assert rc == fg.OK, lib.fomo_last_error(ctx.h).decode()
+            ctx.synchronize()
+            assert G.norm_max_err(out.cpu().numpy(), ref) <= 1e-5
