@@ -1050,16 +1050,17 @@ __device__ __forceinline__ void scan_point(const float4 v, int p, const BoxQ& q,
   }
 }
 
-// Candidates p in [p0, p1), one after the other; `budget` pays one unit per
-// row and per point.  A range of more than kLaneDense points (dense cells)
-// spends the whole budget at once: such samples are searched by a warp.
+// Candidates p in [p0, p1), one after the other.  With BUDGET, `budget` pays
+// one unit per row and per point, and a range of more than kLaneDense points
+// (dense cells) spends it at once: such samples are searched by a warp.
 constexpr int kLaneDense = 48;
-constexpr int kLaneDenseOnly = 0x3ffffffe;  // budget that only a dense range exhausts
-template <bool EXACT>
+template <bool EXACT, bool BUDGET>
 __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p0, int p1, float band, float& best,
                                           float& second, int& bpos, int& borig, double& bD, int& budget) {
-  budget -= (p1 - p0 > kLaneDense && budget <= kLaneDenseOnly) ? 0x3fffffff : 1 + (p1 - p0);
-  if (budget < 0) return;
+  if (BUDGET) {
+    budget -= (p1 - p0 > kLaneDense) ? 0x3fffffff : 1 + (p1 - p0);
+    if (budget < 0) return;
+  }
   for (int p = p0; p < p1; ++p) scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
 }
 
@@ -1067,7 +1068,7 @@ __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p
 // into the grid), nearest first.  A ring, a row or a cell is skipped when its
 // lower bound from the target exceeds the bound (the best squared distance so
 // far, or `band` in the EXACT pass); every loop is bounded by the box's cells.
-template <bool EXACT>
+template <bool EXACT, bool BUDGET>
 __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, const int (&b0)[3], const int (&b1)[3],
                                            const int (&c)[3], const float (&gc)[3], float band, float& best,
                                            float& second, int& bpos, int& borig, double& bD, int& budget) {
@@ -1102,7 +1103,7 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
       const float gz2 = gz * gz;
       const bool zshell = kz == c[2] - s || kz == c[2] + s;
       for (int jy = y0; jy <= y1; ++jy) {
-        if (budget < 0) return;  // out of budget: the warp searches this sample
+        if (BUDGET && budget < 0) return;  // out of budget: a warp searches this sample
         const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
         const float gy = axis_gap(jy, q.ty, g.oy, h);
         const float gyz = fmaf(gy, gy, gz2);
@@ -1118,15 +1119,15 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
             x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
           }
           if (x0 <= x1)
-            lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + x0), __ldg(S.cell_start + rowbase + x1 + 1), band,
+            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + rowbase + x0), __ldg(S.cell_start + rowbase + x1 + 1), band,
                              best, second, bpos, borig, bD, budget);
         } else {
           // a row inside the ring's y-z square: only its two end cells are on the ring
           if (has_l && fmaf(gxl, gxl, gyz) <= bound)
-            lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + xl), __ldg(S.cell_start + rowbase + xl + 1), band,
+            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + rowbase + xl), __ldg(S.cell_start + rowbase + xl + 1), band,
                              best, second, bpos, borig, bD, budget);
           if (has_r && fmaf(gxr, gxr, gyz) <= (EXACT ? bound : best * (1.0f + kRelPrune)))
-            lane_scan<EXACT>(S, q, __ldg(S.cell_start + rowbase + xr), __ldg(S.cell_start + rowbase + xr + 1), band,
+            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + rowbase + xr), __ldg(S.cell_start + rowbase + xr + 1), band,
                              best, second, bpos, borig, bD, budget);
         }
       }
@@ -1162,10 +1163,13 @@ __device__ __forceinline__ bool box_cells(const GridParams& g, const BoxQ& q, in
 constexpr int kLaneBudget = 192;  // rows + points one lane may scan for one sample
 
 // Nearest point strictly inside box q, searched by this lane alone: sorted
-// position and original index, or -1 when the box holds no point.  False when
-// the search ran out of `budget` (dense cells, or a wide box far from the
-// points): a whole warp then searches the sample (warp_search, march_hard).
-__device__ __forceinline__ bool lane_search(const SnapDev& S, const BoxQ& q, int& pos, int& orig, int budget) {
+// position and original index, or -1 when the box holds no point.  With
+// BUDGET, false when the search ran out of kLaneBudget (dense cells, or a
+// wide box far from the points): a whole warp then searches the sample
+// (warp_search, march_hard).
+template <bool BUDGET>
+__device__ __forceinline__ bool lane_search(const SnapDev& S, const BoxQ& q, int& pos, int& orig) {
+  int budget = kLaneBudget;
   pos = -1;
   orig = -1;
   int b0[3], b1[3], c[3];
@@ -1174,22 +1178,29 @@ __device__ __forceinline__ bool lane_search(const SnapDev& S, const BoxQ& q, int
   float best = FLT_MAX, second = FLT_MAX;
   int bpos = -1, borig = -1;
   double bD = DBL_MAX;
-  lane_rings<false>(S, q, b0, b1, c, gc, 0.0f, best, second, bpos, borig, bD, budget);
-  if (budget < 0) return false;
+  lane_rings<false, BUDGET>(S, q, b0, b1, c, gc, 0.0f, best, second, bpos, borig, bD, budget);
+  if (BUDGET && budget < 0) return false;
   if (bpos < 0) return true;
   if (second <= best * (1.0f + kRelTie)) {
     // possible FP64 tie (or an exact FP32 tie): re-rank the contenders
     float fb = FLT_MAX, fs = FLT_MAX;
     int p2 = -1, o2 = 0x7fffffff;
     double D2 = DBL_MAX;
-    lane_rings<true>(S, q, b0, b1, c, gc, best * (1.0f + kRelTie), fb, fs, p2, o2, D2, budget);
-    if (budget < 0) return false;
+    lane_rings<true, BUDGET>(S, q, b0, b1, c, gc, best * (1.0f + kRelTie), fb, fs, p2, o2, D2, budget);
+    if (BUDGET && budget < 0) return false;
     bpos = p2;
     borig = o2;
   }
   pos = bpos;
   orig = borig;
   return true;
+}
+
+// lane_search without a budget, out of line: for the rare sample that finds
+// the hard queue full (a second inlined copy of the ring walks would crowd
+// the deferred kernel's instruction cache).
+__device__ __noinline__ void lane_search_full(const SnapDev& S, const BoxQ q, int& pos, int& orig) {
+  lane_search<false>(S, q, pos, orig);
 }
 
 // Warp-collective walk over the same rings as lane_rings for one sample (q
@@ -1493,6 +1504,58 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_split(MarchArgs a, c
   }
 }
 
+// Phase 1 of march_deferred: samples [0, nsamp) of the staged records, one
+// per lane, each searched by its lane; results staged in sp / sv.  With
+// BUDGET (a short queue: latency matters), a sample in dense cells or over the
+// budget goes to the hard queue (a whole warp searches it in march_hard) and
+// adds nothing here.  A long queue has no budget: 32 lanes on 32 samples keep
+// more loads in flight than a warp on one, and its walk has no budget checks.
+template <bool BUDGET>
+__device__ __forceinline__ void deferred_search(const MarchArgs& a, int kind, int nsamp, int start, int incl,
+                                                int excl, const DeferredRec& rec, const RayCtx& mine, int* sp,
+                                                float* sv) {
+  const int lane = threadIdx.x & 31;
+  for (int t0 = 0; t0 < nsamp; t0 += 32) {
+    const int t = t0 + lane;
+    const int own = warp_owner(incl, start + t) & 31;  // the record lane holding flattened sample t
+    const unsigned oy = __shfl_sync(kFull, rec.y, own);
+    const unsigned oz = __shfl_sync(kFull, rec.z, own), ow = __shfl_sync(kFull, rec.w, own);
+    const int oe = __shfl_sync(kFull, excl, own);
+    const RayCtx r = shfl_ray(mine, own);
+    bool hard = false;
+    int k = 0, p = -1, o = -1;
+    if (t < nsamp) {
+      k = (int)oy + nth_set_bit(oz, ow, start + t - oe);
+      hard = !lane_search<BUDGET>(a.snap, exact_box(r, k), p, o);
+    }
+    if (BUDGET) {
+      const unsigned hm = __ballot_sync(kFull, hard);
+      unsigned long long hb = 0;
+      if (hm && lane == 0) hb = atomicAdd(a.counter + kCtrHard, (unsigned long long)__popc(hm));
+      hb = __shfl_sync(kFull, hb, 0);
+      if (hard) {
+        const int64_t slot = (int64_t)hb + __popc(hm & ((1u << lane) - 1u));
+        if (slot < a.hard_cap) {
+          a.hard[slot] = make_uint2(r.item, (unsigned)k);
+          p = -1;  // its neighbour and emission come from march_hard
+        } else {
+          lane_search_full(a.snap, exact_box(r, k), p, o);  // queue full: finish here
+          hard = false;
+        }
+      }
+      if (a.stats && hm && lane == 0) atomicAdd(a.stats + kStatHard, (unsigned long long)__popc(hm));
+    }
+    if (t < nsamp) {
+      if (hard) {
+        sp[t] = -1;
+        sv[t] = 0.0f;
+      } else {
+        store_deferred(a, r, k, kind, p, o, sp + t, sv + t);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride, int kind) {
   __shared__ int spos[kWarps][kDefBatch];    // neighbour (sorted position) of each staged sample
@@ -1507,7 +1570,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
   // warp of the grid gets a share (a small render has few records)
   const int64_t nwarps = (int64_t)gridDim.x * kWarps;
   const int grab = (int)max((int64_t)1, min((int64_t)32, nrec / nwarps));
-  const bool short_queue = nrec < 32 * nwarps;
+  // a short queue (a small render: latency matters) takes the budgeted search
+  const bool budgeted = a.hard_cap > 0 && nrec < 256 * nwarps;
   for (;;) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(a.counter + kCtrDeferredHead, (unsigned long long)grab);
@@ -1530,51 +1594,11 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
       const unsigned fits = __ballot_sync(kFull, lane >= r0 && incl - start <= kDefBatch);
       const int r1 = r0 + max(__popc(fits), 1);
       const int nsamp = __shfl_sync(kFull, incl, r1 - 1) - start;
-      // 1. one sample per lane: its record, ray and box, then its own search.
-      // A sample in dense cells, or (when the queue is short and latency
-      // matters) one over the budget, goes to the hard queue (a whole warp
-      // searches it in march_hard) and adds nothing here; with a long queue,
-      // 32 lanes on 32 samples keep more loads in flight than a warp on one.
-      const int budget = a.hard_cap <= 0 ? 0x7fffffff : (short_queue ? kLaneBudget : kLaneDenseOnly);
-      for (int t0 = 0; t0 < nsamp; t0 += 32) {
-        const int t = t0 + lane;
-        const int own = warp_owner(incl, start + t) & 31;  // the record lane holding flattened sample t
-        const unsigned oy = __shfl_sync(kFull, rec.y, own);
-        const unsigned oz = __shfl_sync(kFull, rec.z, own), ow = __shfl_sync(kFull, rec.w, own);
-        const int oe = __shfl_sync(kFull, excl, own);
-        const RayCtx r = shfl_ray(mine, own);
-        bool hard = false;
-        int k = 0, p = -1, o = -1;
-        BoxQ q{};
-        if (t < nsamp) {
-          k = (int)oy + nth_set_bit(oz, ow, start + t - oe);
-          q = exact_box(r, k);
-          hard = !lane_search(a.snap, q, p, o, budget);
-        }
-        const unsigned hm = __ballot_sync(kFull, hard);
-        unsigned long long hb = 0;
-        if (hm && lane == 0) hb = atomicAdd(a.counter + kCtrHard, (unsigned long long)__popc(hm));
-        hb = __shfl_sync(kFull, hb, 0);
-        if (hard) {
-          const int64_t slot = (int64_t)hb + __popc(hm & ((1u << lane) - 1u));
-          if (slot < a.hard_cap) {
-            a.hard[slot] = make_uint2(r.item, (unsigned)k);
-            p = -1;  // its neighbour and emission come from march_hard
-          } else {
-            lane_search(a.snap, q, p, o, 0x7fffffff);  // queue full: finish here
-            hard = false;
-          }
-        }
-        if (t < nsamp) {
-          if (hard) {
-            spos[w][t] = -1;
-            svlos[w][t] = 0.0f;
-          } else {
-            store_deferred(a, r, k, kind, p, o, spos[w] + t, svlos[w] + t);
-          }
-        }
-        if (a.stats && hm && lane == 0) atomicAdd(a.stats + kStatHard, (unsigned long long)__popc(hm));
-      }
+      // 1. one sample per lane: its record, ray and box, then its own search
+      if (budgeted)
+        deferred_search<true>(a, kind, nsamp, start, incl, excl, rec, mine, spos[w], svlos[w]);
+      else
+        deferred_search<false>(a, kind, nsamp, start, incl, excl, rec, mine, spos[w], svlos[w]);
       __syncwarp();
       // 2. their emission, record by record
       for (int rr = r0; rr < r1; ++rr) {
