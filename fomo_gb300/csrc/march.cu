@@ -1410,10 +1410,12 @@ __device__ __forceinline__ void add_emission(const MarchArgs& a, const RayCtx& r
   }
 }
 
-// The record at position ri of the deferred queue: the first pass's records
-// from the front of the buffer, then the overflow records from the back.
-__device__ __forceinline__ DeferredRec deferred_at(const MarchArgs& a, int64_t nfront, int64_t ri) {
-  return ri < nfront ? a.deferred[ri] : a.deferred[a.deferred_cap - 1 - (ri - nfront)];
+// The record at position ri of the deferred queue: the overflow records from
+// the back of the buffer first (what their parts left is mostly dense cells,
+// the slowest searches: started early, they do not make the kernel's tail),
+// then the first pass's records from the front.
+__device__ __forceinline__ DeferredRec deferred_at(const MarchArgs& a, int64_t nback, int64_t ri) {
+  return ri < nback ? a.deferred[a.deferred_cap - 1 - ri] : a.deferred[ri - nback];
 }
 
 // A deferred sample's result: its NN index, and its neighbour and LOS speed
@@ -1565,7 +1567,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
   // written by the march and march_split; the two ends of the buffer never meet
   // (at most one record per segment)
   const int64_t nfront = min((int64_t)a.counter[kCtrDeferred], a.deferred_cap);
-  const int64_t nrec = nfront + min((int64_t)a.counter[kCtrOverflow], a.deferred_cap - nfront);
+  const int64_t nback = min((int64_t)a.counter[kCtrOverflow], a.deferred_cap - nfront);
+  const int64_t nrec = nfront + nback;
   // records per grab: 32, or fewer when the queue is short, so that every
   // warp of the grid gets a share (a small render has few records)
   const int64_t nwarps = (int64_t)gridDim.x * kWarps;
@@ -1579,7 +1582,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a
     if ((int64_t)base >= nrec) return;
     const int64_t ri = (int64_t)base + lane;
     DeferredRec rec = make_uint4(0u, 0u, 0u, 0u);
-    if (lane < grab && ri < nrec) rec = deferred_at(a, nfront, ri);
+    if (lane < grab && ri < nrec) rec = deferred_at(a, nback, ri);
     const int cnt = __popc(rec.z) + __popc(rec.w);
     const int incl = warp_incl_scan(cnt);
     const int excl = incl - cnt;
