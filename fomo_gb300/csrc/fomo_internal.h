@@ -79,9 +79,11 @@ struct LineDesc {
 // of deferred-sample records written from the front of the buffer, the
 // deferred-record queue head, the number of overflow records written from the
 // back (segments whose capsule held too many points), their queue head, the
-// number of hard samples queued for a warp each, their queue head.
+// number of hard samples queued for a warp each, their queue head, the ray
+// queue head of the emission pass of the two-pass spectral march.
 enum MarchCounter {
-  kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrOverflow, kCtrOverflowHead, kCtrHard, kCtrHardHead, kCtrCount
+  kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrOverflow, kCtrOverflowHead, kCtrHard, kCtrHardHead, kCtrShade,
+  kCtrCount
 };
 
 // One segment whose samples the march's first search pass could not resolve:
@@ -104,6 +106,7 @@ struct MarchArgs {
   uint2* hard;                   // deferred samples (work item, sample) for a whole warp each, or null
   int64_t hard_cap;              // its capacity (0: every deferred sample is searched by one lane)
   int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
+  int32_t* npos;                 // spectral two-pass march: neighbour per (work item - item_base, sample), or null
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
   unsigned int* err;             // device error word (bounds-check builds)

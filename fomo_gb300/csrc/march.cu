@@ -62,6 +62,8 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMinCtas = 4;  // resident CTAs per SM: 16 warps of latency hiding at <= 128 registers
+constexpr int kMinCtasSearch = 5;  // the search-only pass: 20 warps at <= 102 registers (shared memory allows 5)
+constexpr int kMinCtasShade = 8;   // the emission-only pass: 32 warps at <= 64 registers
 constexpr float kRelTie = 4e-6f;      // FP32 distance ambiguity band (>> FP32 + FP64 error)
 constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
@@ -180,12 +182,13 @@ __device__ __forceinline__ bool ray_of_item(const MarchArgs& a, const double3* k
 }
 
 // Warp-collective: the next ray of the work queue (items item_base ..
-// total_items - 1), false when the queue is drained.
-__device__ __forceinline__ bool next_ray(const MarchArgs& a, const double3* ktab, int ktab_stride, RayCtx& r) {
+// total_items - 1, head counter `ctr`), false when the queue is drained.
+__device__ __forceinline__ bool next_ray(const MarchArgs& a, const double3* ktab, int ktab_stride, RayCtx& r,
+                                         int ctr = kCtrRays) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long item = 0;
-    if (lane == 0) item = atomicAdd(a.counter + kCtrRays, 1ull);
+    if (lane == 0) item = atomicAdd(a.counter + ctr, 1ull);
     item = __shfl_sync(kFull, item, 0) + (unsigned long long)a.item_base;
     if ((int64_t)item >= a.total_items) return false;
     if (ray_of_item(a, ktab, ktab_stride, (int64_t)item, r)) return true;
@@ -818,19 +821,55 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // ---------------------------------------------------------------------------
-// Spectroscopic march: NL lines x up to NB 32-bin windows per line; lane
-// `lane` owns bins wstart + 32 m + lane of each line.
+// Search pass of the two-pass spectral march: each sample's neighbour (sorted
+// position, -1 for none or deferred) into a.npos, [work item - item_base][k],
+// streamed past L2; the NN indices when asked for.  march_spectral<.., true>
+// then bins the emission from these positions.
 // ---------------------------------------------------------------------------
-template <int NL, int NB>
-__global__ void __launch_bounds__(kThreads, kMinCtas) march_spectral(MarchArgs a, const double3* __restrict__ ktab,
-                                                           int ktab_stride) {
+__global__ void __launch_bounds__(kThreads, kMinCtasSearch) march_search(MarchArgs a, const double3* __restrict__ ktab,
+                                                               int ktab_stride) {
   __shared__ SegSmem segs[kWarps];
-  __shared__ float4 runs[kWarps][32][NL];  // a chunk's runs: (peak x length, 2/w, Doppler term) per line
-  const int w = threadIdx.x >> 5;
-  SegSmem& sm = segs[w];
+  SegSmem& sm = segs[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   RayCtx r;
   while (next_ray(a, ktab, ktab_stride, r)) {
+    const ViewDesc* V = a.views + r.v;
+    const int nz = V->nz;
+    int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+    const int64_t ray = (int64_t)r.i * V->nx + r.j;
+    int32_t* npos = a.npos + ((int64_t)r.item - a.item_base) * ktab_stride;
+    for (int s0 = 0; s0 < nz; s0 += kSeg) {
+      int posv[2], origv[2];
+      segment_search(a, r, s0, nz, sm, posv, origv);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = s0 + 32 * h + lane;
+        if (k < nz) {
+          __stcs(npos + k, h ? posv[1] : posv[0]);
+          if (nnout) nnout[ray * nz + k] = h ? origv[1] : origv[0];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Spectroscopic march: NL lines x up to NB 32-bin windows per line; lane
+// `lane` owns bins wstart + 32 m + lane of each line.
+// ---------------------------------------------------------------------------
+// SHADE: the neighbours come from the position buffer written by
+// march_search (a.npos) instead of the search itself; the emission code and
+// its arithmetic are the same.
+template <int NL, int NB, bool SHADE>
+__global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
+    march_spectral(MarchArgs a, const double3* __restrict__ ktab, int ktab_stride) {
+  __shared__ SegSmem segs[SHADE ? 1 : kWarps];
+  __shared__ float4 runs[kWarps][32][NL];  // a chunk's runs: (peak x length, 2/w, Doppler term) per line
+  const int w = threadIdx.x >> 5;
+  SegSmem& sm = segs[SHADE ? 0 : w];
+  const int lane = threadIdx.x & 31;
+  RayCtx r;
+  while (next_ray(a, ktab, ktab_stride, r, SHADE ? kCtrShade : kCtrRays)) {
     const ViewDesc* V = a.views + r.v;
     const int nz = V->nz, L = V->L, nx = V->nx;
     const float ux = V->ux, uy = V->uy, uz = V->uz;
@@ -857,11 +896,17 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_spectral(MarchArgs a
         lam[l][m] = (m < nw[l] && il < L) ? __ldg(LD[l].lam + il) : 3.0e30f;
       }
     }
-    int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+    int32_t* nnout = (!SHADE && a.nn_idx) ? a.nn_idx[r.v] : nullptr;
     const int64_t ray = (int64_t)r.i * nx + r.j;
+    const int32_t* npos = SHADE ? a.npos + ((int64_t)r.item - a.item_base) * ktab_stride : nullptr;
     for (int s0 = 0; s0 < nz; s0 += kSeg) {
       int posv[2], origv[2];
-      segment_search(a, r, s0, nz, sm, posv, origv);
+      if (SHADE) {
+        posv[0] = s0 + lane < nz ? __ldcs(npos + s0 + lane) : -1;
+        posv[1] = s0 + 32 + lane < nz ? __ldcs(npos + s0 + 32 + lane) : -1;
+      } else {
+        segment_search(a, r, s0, nz, sm, posv, origv);
+      }
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
         const int k = s0 + 32 * h + lane;
@@ -1707,8 +1752,27 @@ cudaError_t launch_first_pass(const MarchArgs& a, const double3* ktab, int ktab_
     return cudaErrorInvalidValue;
   }
   const int nb = max_windows < 1 ? 1 : max_windows;
+  if (a.npos) {
+    // two passes: the search, then the emission from the stored positions
+    cudaError_t e = launch_persistent(march_search, a, ktab, ktab_stride, sm_count, s, 0);
+    if (e != cudaSuccess) return e;
+#define FOMO_SHADE(NL_, NB_) \
+  if (a.nlines <= NL_ && nb <= NB_) return launch_persistent(march_spectral<NL_, NB_, true>, a, ktab, ktab_stride, sm_count, s, 0)
+    FOMO_SHADE(1, 1);
+    FOMO_SHADE(1, 2);
+    FOMO_SHADE(1, 4);
+    FOMO_SHADE(1, 8);
+    FOMO_SHADE(2, 1);
+    FOMO_SHADE(2, 2);
+    FOMO_SHADE(2, 4);
+    FOMO_SHADE(4, 1);
+    FOMO_SHADE(4, 2);
+    FOMO_SHADE(4, 4);
+#undef FOMO_SHADE
+    return cudaErrorInvalidValue;
+  }
 #define FOMO_SPEC(NL_, NB_) \
-  if (a.nlines <= NL_ && nb <= NB_) return launch_persistent(march_spectral<NL_, NB_>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint)
+  if (a.nlines <= NL_ && nb <= NB_) return launch_persistent(march_spectral<NL_, NB_, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint)
   FOMO_SPEC(1, 1);
   FOMO_SPEC(1, 2);
   FOMO_SPEC(1, 4);

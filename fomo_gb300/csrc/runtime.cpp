@@ -737,6 +737,9 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     G.o_def = L.take(sizeof(DeferredRec) * (size_t)G.deferred_cap);
     G.hard_cap = hard_capacity(items, G.maxnz);
     G.o_hard = L.take(sizeof(uint2) * (size_t)G.hard_cap);
+    // spectral NN: the search and the emission run as two passes through a
+    // neighbour buffer (each pass at its own occupancy)
+    G.o_npos = (G.method == FOMO_METHOD_NN && !G.imaging) ? L.take(sizeof(int32_t) * (size_t)items * G.maxnz) : 0;
     G.o_s2 = G.method == FOMO_METHOD_THOMSON ? L.take(sizeof(float) * (size_t)G.nv * snap.n) : 0;
   }
   plan->dev_bytes = L.off;
@@ -902,6 +905,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.deferred_cap = G.deferred_cap;
     a.hard = reinterpret_cast<uint2*>(db + G.o_hard);
     a.hard_cap = G.hard_cap;
+    a.npos = G.o_npos ? reinterpret_cast<int32_t*>(db + G.o_npos) : nullptr;
     a.nn_idx = G.any_nn ? reinterpret_cast<int32_t* const*>(db + G.o_nnp) : nullptr;
     a.s2 = s2;
     a.totpol = G.totpol;
