@@ -426,15 +426,15 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                          "bytes_per_sample": bps,
-                         "kernel": "march_spectral<4,1> (first search pass + emission sums) + march_split "
-                                   "(overflowing segments) + march_deferred (the samples the first pass "
-                                   "leaves) + march_hard (deferred samples over the one-lane budget), "
-                                   "timed together"},
+                         "kernel": "march_search (neighbour search, positions to a buffer) + "
+                                   "march_spectral<4,1,shade> (emission from the positions) + march_split "
+                                   "(overflowing segments) + march_deferred (the samples the search leaves) + "
+                                   "march_hard (deferred samples over the one-lane budget), timed together"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            # per step: view init, view extents, view finalize, first-pass march, overflow split, deferred march,
+            # per step: view init, view extents, view finalize, search, emission, overflow split, deferred march,
             # hard-sample march
-            "gpu_launches": 7 * args.steps,
+            "gpu_launches": 8 * args.steps,
             "serving": serving,
         }
         print(json.dumps(out))
