@@ -62,13 +62,14 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMinCtas = 4;  // resident CTAs per SM: 16 warps of latency hiding at <= 128 registers
-constexpr int kMinCtasSearch = 5;  // the search-only pass: 20 warps at <= 102 registers (shared memory allows 5)
+constexpr int kMinCtasSearch = 7;   // the search-only pass: 28 warps at <= 72 registers (31 KB shared per CTA)
 constexpr int kMinCtasShade = 8;   // the emission-only pass: 32 warps at <= 64 registers
+constexpr int kMinCtasImaging = 5; // imaging / Thomson first pass: 20 warps at <= 102 registers
 constexpr float kRelTie = 4e-6f;      // FP32 distance ambiguity band (>> FP32 + FP64 error)
 constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
 constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
-constexpr int kSegCap = 256;          // candidates per segment
+constexpr int kSegCap = 176;          // candidates per segment (sized so that 7 search CTAs fit an SM)
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule beyond which it is deferred
 constexpr float kRScale = 1.0f;       // gather radius in local point spacings
 
@@ -995,7 +996,7 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
 // reduced across the warp per 32-sample chunk, Kahan-accumulated per ray.
 // ---------------------------------------------------------------------------
 template <int NL, bool THOMSON>
-__global__ void __launch_bounds__(kThreads, kMinCtas) march_imaging(MarchArgs a, const double3* __restrict__ ktab,
+__global__ void __launch_bounds__(kThreads, kMinCtasImaging) march_imaging(MarchArgs a, const double3* __restrict__ ktab,
                                                           int ktab_stride) {
   __shared__ SegSmem segs[kWarps];
   SegSmem& sm = segs[threadIdx.x >> 5];
