@@ -65,6 +65,7 @@ constexpr int kMinCtas = 4;  // resident CTAs per SM: 16 warps of latency hiding
 constexpr int kMinCtasSearch = 7;   // the search-only pass: 28 warps at <= 72 registers (31 KB shared per CTA)
 constexpr int kMinCtasShade = 8;   // the emission-only pass: 32 warps at <= 64 registers
 constexpr int kMinCtasImaging = 5; // imaging / Thomson first pass: 20 warps at <= 102 registers
+constexpr int kMinCtasDeferred = 8; // one-lane ring walks wait on dependent loads: 32 warps (64 registers, some spill)
 constexpr float kRelTie = 4e-6f;      // FP32 distance ambiguity band (>> FP32 + FP64 error)
 constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
@@ -1604,7 +1605,7 @@ __device__ __forceinline__ void deferred_search(const MarchArgs& a, int kind, in
   }
 }
 
-__global__ void __launch_bounds__(kThreads, kMinCtas) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
+__global__ void __launch_bounds__(kThreads, kMinCtasDeferred) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride, int kind) {
   __shared__ int spos[kWarps][kDefBatch];    // neighbour (sorted position) of each staged sample
   __shared__ float svlos[kWarps][kDefBatch]; // and its LOS speed (spectral)
