@@ -1,6 +1,14 @@
-// K4/K5/K6: the fused ray march (fomo-c/src/fomo-nearestneighbour.cpp:145-229
-// and fomo-thomson.cpp:268-343), one warp per ray, persistent over a queue of
+// K4/K5/K6: the ray march (fomo-c/src/fomo-nearestneighbour.cpp:145-229 and
+// fomo-thomson.cpp:268-343), one warp per ray, persistent over a queue of
 // (view, ray) work items so that many views and requests share one launch.
+//
+// Kernels, in stream order: the first pass (march_search for spectral renders,
+// which stores each sample's neighbour in a buffer, then
+// march_spectral<.., shade> which bins the emission from it; march_imaging for
+// imaging and Thomson, which does both; march_spectral<.., fused> on the
+// no-allocation path), march_split (segments whose capsule overflowed),
+// march_deferred (samples the first pass could not resolve, one lane each)
+// and march_hard (deferred samples over a lane's budget, one warp each).
 //
 // Per ray: the FP64 per-ray terms of the derotation (x cos b cos l + y sin l,
 // -x cos b sin l + y cos l, -x sin b) are formed once; each LOS sample adds the
@@ -31,10 +39,11 @@
 //  5. defer: every other sample (about 1 %) contributes nothing here; its
 //     segment is recorded.  A segment whose capsule held more than kSegCap
 //     points is first searched again in parts of 32 or 16 samples
-//     (march_split); a third kernel (march_deferred) then searches each
-//     such sample on one lane -- rings of grid cells around the sample's cell,
-//     clipped to its box (corners rounded from FP64 as the reference does),
-//     nearest ring first, stopped by a distance bound -- then adds its emission.
+//     (march_split); march_deferred then searches each such sample on one
+//     lane -- rings of grid cells around the sample's cell, clipped to its box
+//     (corners rounded from FP64 as the reference does), nearest ring first,
+//     stopped by a distance bound -- or hands it to march_hard, where a whole
+//     warp walks the same rings; either adds the sample's emission.
 // Either way the chosen neighbour is the FP64 argmin strictly inside the box.
 //
 // Spectroscopic mode: equal neighbours of consecutive samples are merged into
@@ -45,8 +54,9 @@
 // Gaussian can exceed 2^-64 of its peak; the others are written as 0) in a
 // per-chunk FP32 partial, folded into the per-ray sum with Kahan compensation.
 // Imaging (L = 1) and Thomson (pB) add per-sample values through a warp
-// reduction.  One warp owns one ray in the first pass (no atomics); the
-// deferred samples' emission is added with atomics afterwards.
+// reduction.  One warp owns one ray in the first pass and in the emission pass
+// (no atomics); the deferred samples' emission is added with atomics
+// afterwards.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
