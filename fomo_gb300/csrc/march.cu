@@ -76,6 +76,7 @@ constexpr int kMinCtasSearch = 7;   // the search-only pass: 28 warps at <= 72 r
 constexpr int kMinCtasShade = 8;   // the emission-only pass: 32 warps at <= 64 registers
 constexpr int kMinCtasImaging = 5; // imaging / Thomson first pass: 20 warps at <= 102 registers
 constexpr int kMinCtasDeferred = 8; // one-lane ring walks wait on dependent loads: 32 warps (64 registers, some spill)
+constexpr int kMinCtasSplit = 6;    // overflow parts: 24 warps at <= 85 registers (33 KB shared per CTA allows 6)
 constexpr float kRelTie = 4e-6f;      // FP32 distance ambiguity band (>> FP32 + FP64 error)
 constexpr float kRelPrune = 1e-5f;    // pruning slack on the squared distance
 constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning error < 1e-3 cell)
@@ -1500,7 +1501,7 @@ __device__ __forceinline__ void store_deferred(const MarchArgs& a, const RayCtx&
 // emission of the samples it resolves and rewrites the record with the
 // samples still unresolved, for march_deferred.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, kMinCtas) march_split(MarchArgs a, const double3* __restrict__ ktab,
+__global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs a, const double3* __restrict__ ktab,
                                                         int ktab_stride, int kind) {
   __shared__ SegSmem segs[kWarps];
   __shared__ int spos[kWarps][kSeg];
