@@ -422,7 +422,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "line-samples/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": len(e2e_times), "stat": "median",
                     "ms_per_step": 1e3 * e2e_med, "ms_min": 1e3 * float(np.min(e2e_times)),
-                    "ms_max": 1e3 * float(np.max(e2e_times))},
+                    "ms_max": 1e3 * float(np.max(e2e_times)), "ms_steps": [1e3 * t for t in e2e_times]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                          "bytes_per_sample": bps,
