@@ -738,8 +738,16 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     G.hard_cap = hard_capacity(items, G.maxnz);
     G.o_hard = L.take(sizeof(uint2) * (size_t)G.hard_cap);
     // spectral NN: the search and the emission run as two passes through a
-    // neighbour buffer (each pass at its own occupancy)
-    G.o_npos = (G.method == FOMO_METHOD_NN && !G.imaging) ? L.take(sizeof(int32_t) * (size_t)items * G.maxnz) : 0;
+    // neighbour buffer
+    // (each pass at its own occupancy); at most ctx->npos_cap entries, the
+    // launch marching in item chunks beyond that
+    G.npos_items = 0;
+    G.o_npos = 0;
+    if (G.method == FOMO_METHOD_NN && !G.imaging) {
+      const int64_t cap_items = std::max<int64_t>(1, ctx->npos_cap / G.maxnz);
+      G.npos_items = std::min<int64_t>(items, cap_items);
+      G.o_npos = L.take(sizeof(int32_t) * (size_t)G.npos_items * G.maxnz);
+    }
     G.o_s2 = G.method == FOMO_METHOD_THOMSON ? L.take(sizeof(float) * (size_t)G.nv * snap.n) : 0;
   }
   plan->dev_bytes = L.off;
@@ -920,14 +928,22 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     } else if (e == cudaSuccess) {
       // the march over view ranges: each range's rays are a contiguous run of
       // work items, with the work counters cleared before it
+      // a view range marches in item chunks when its neighbour buffer would
+      // exceed the buffer's capacity (the buffer is indexed from item_base)
       const std::vector<int> cuts = view_ranges(G, done != nullptr, range_cost);
+      bool first = true;
       for (size_t k = 0; k + 1 < cuts.size() && e == cudaSuccess && rc == FOMO_OK; ++k) {
-        if (k > 0) e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * kCtrCount, s);
-        a.item_base = G.item_off[cuts[k]];
-        a.total_items = G.item_off[cuts[k + 1]];
-        if (e == cudaSuccess)
-          e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
-                           G.method == FOMO_METHOD_THOMSON || G.imaging);
+        const int64_t i0 = G.item_off[cuts[k]], i1 = G.item_off[cuts[k + 1]];
+        const int64_t step = G.npos_items > 0 ? G.npos_items : (i1 - i0);
+        for (int64_t b = i0; b < i1 && e == cudaSuccess; b += step) {
+          if (!first) e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * kCtrCount, s);
+          first = false;
+          a.item_base = b;
+          a.total_items = std::min(i1, b + step);
+          if (e == cudaSuccess)
+            e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
+                             G.method == FOMO_METHOD_THOMSON || G.imaging);
+        }
         if (e == cudaSuccess && done) rc = (*done)(G, cuts[k], cuts[k + 1]);
       }
     }
@@ -1018,6 +1034,10 @@ int fomo_ctx_create(int device, size_t hbm_budget_bytes, fomo_ctx** out) {
     return FOMO_EDEVICE;
   }
   if (const char* tc = std::getenv("FOMO_TUNE_CACHE")) load_tune_cache(ctx, tc);
+  if (const char* nc = std::getenv("FOMO_NPOS_CAP")) {
+    const long long v = std::atoll(nc);  // neighbour-buffer entries (4 B each) per launch
+    if (v > 0) ctx->npos_cap = v;
+  }
   if (const char* ms = std::getenv("FOMO_MARCH_STATS")) {
     if (ms[0] == '1' && cudaMalloc(&ctx->march_stats, sizeof(unsigned long long) * kStatCount) == cudaSuccess)
       cudaMemset(ctx->march_stats, 0, sizeof(unsigned long long) * kStatCount);

@@ -102,6 +102,7 @@ struct PlanGroup {
   size_t o_hard = 0;
   int64_t hard_cap = 0;      // hard-sample queue entries
   size_t o_npos = 0;         // spectral two-pass march: a neighbour per (work item, sample), or 0
+  int64_t npos_items = 0;    // work items the neighbour buffer holds (the launch marches in chunks of these)
   std::vector<int64_t> item_off;  // first work item of each view (nv + 1 entries)
   std::vector<double> vcost;      // LOS samples + output cells of each view
   size_t out_bytes = 0;           // cube bytes of all its requests
@@ -150,6 +151,7 @@ struct fomo_ctx {
   fomo::Arena out_arena;     // device cubes of host-output renders
   std::vector<fomo::ViewReadback> view_readback;
   double cell_occupancy = 2.0;  // target points per grid cell
+  int64_t npos_cap = int64_t(1) << 31;  // neighbour-buffer entries per launch (FOMO_NPOS_CAP): 8 GiB
   int tile_w = 0, tile_h = 0, blocks_per_sm = 0;
   bool time_march = true;
   float last_ms = 0.0f;

@@ -81,6 +81,37 @@ def test_host_batch_downloads_in_chunks_same_as_alone(ctx):
     ctx.drop_snapshot(sid)
 
 
+def test_small_neighbour_buffer_marches_in_item_chunks(monkeypatch):
+    """FOMO_NPOS_CAP bounds the spectral march's neighbour buffer; a launch then
+    marches in chunks of work items.  Neighbour indices must equal those of an
+    unchunked render, and cubes must match up to the order of the deferred
+    passes' atomic additions; a host batch (view ranges + chunks) as well."""
+    s = synth.loop_snapshot(24, seed=5)
+    t = synth.line_table()
+    width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+    views = [(0.3, 0.1), (1.0, -0.2), (1.7, 0.25)]
+
+    def run(c):
+        sid, tid = c.snapshot(s), c.table(t)
+        cube, idx, info = c.render(c.request(sid, tid, fg.METHOD_NN, 48, 40, 96, 32, 0.6, -0.15, width),
+                                   want_idx=True)
+        cubes, infos = c.render_batch([c.request(sid, tid, fg.METHOD_NN, 40, 36, 80, 24, l, b, width)
+                                       for (l, b) in views])
+        return cube, idx, info, cubes, infos
+
+    with fg.Context(0) as c1:
+        ref = run(c1)
+    monkeypatch.setenv("FOMO_NPOS_CAP", str(96 * 37))  # 37 work items per chunk
+    with fg.Context(0) as c2:
+        got = run(c2)
+    np.testing.assert_array_equal(got[1], ref[1])
+    assert G.norm_max_err(got[0].ravel(), ref[0].ravel()) <= 1e-6
+    assert got[2].as_dict() == ref[2].as_dict()
+    for a, b, ia, ib in zip(got[3], ref[3], got[4], ref[4]):
+        assert G.norm_max_err(a.ravel(), b.ravel()) <= 1e-6
+        assert ia.as_dict() == ib.as_dict()
+
+
 def test_server_same_alone_and_in_mix():
     rng = np.random.default_rng(17)
     with fg.Server(0) as srv:
