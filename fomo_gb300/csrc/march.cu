@@ -83,7 +83,7 @@ constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning e
 constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
 constexpr int kSegCap = 176;          // candidates per segment (sized so that 7 search CTAs fit an SM)
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule beyond which it is deferred
-constexpr float kRScale = 1.0f;       // gather radius in local point spacings
+constexpr float kRScale = 0.9f;       // gather radius in local point spacings
 
 
 struct __align__(16) SegSmem {
