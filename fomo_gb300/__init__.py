@@ -58,8 +58,7 @@ class SnapshotInfo(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int),
-                ("tile_rays", ctypes.c_int)]
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int)]
 
 
 class RequestStats(ctypes.Structure):
@@ -311,7 +310,7 @@ class Server:
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, max_inflight: int = 0):
         self._L = lib()
-        cfg = ServerConfig(device, hbm_budget, max_inflight, 0)
+        cfg = ServerConfig(device, hbm_budget, max_inflight)
         h = ctypes.c_void_p()
         rc = self._L.fomo_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != OK:

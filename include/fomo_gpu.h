@@ -231,7 +231,6 @@ typedef struct {
   int device;
   size_t hbm_budget_bytes;  /* admission limit for in-flight request buffers (0 = 50% of free) */
   int max_inflight;         /* requests resident on the device at once (0 = 64) */
-  int tile_rays;            /* rays of one request scheduled per step (0 = whole request) */
 } fomo_server_config;
 
 typedef struct {
