@@ -12,7 +12,8 @@ value      : line-samples/s of the batched render, inputs resident in HBM, L2
              flushed (256 MiB write) before each timed step, CUDA events.
 plain_*    : the plain single-request GPU render (512x512, 128 bins, 512
              samples, l in {0, 30, 60 deg}, b = 0), one request per call --
-             the denominator of the batched-vs-plain metric.
+             the denominator of the batched-vs-plain metric; and the batched
+             workload's own 256 requests rendered one per call (identical work).
 e2e        : the same batch through the C ABI with pinned host buffers: upload
              the snapshot, build the index, emissivity, render, download every
              cube, per step (median of 5 steps).
@@ -20,10 +21,11 @@ roofline   : the march kernel's algorithmic bytes / its event-timed duration
              against the measured HBM copy bandwidth.
 cpu_baseline: the oracle (C restatement, OpenMP on all host cores) on a bounded
              sample of rows of the plain configuration.
-serving    : a Poisson stream of mixed requests (200/s, 8 resident snapshots of
-             0.5M-8M points, random views, pixels, lambda bins and lines) through
-             the continuous-batching server: p50/p90/p99 latency, throughput,
-             and the same requests alone for comparison (N = 1 only).
+serving    : Poisson streams of mixed requests (200/s, and 400/s and 800/s above
+             the server's one-at-a-time capacity; 8 resident snapshots of 0.5M-8M
+             points, random views, pixels, lambda bins and lines) through the
+             continuous-batching server: p50/p90/p99 latency and throughput per
+             rate, and the same requests alone for comparison (N = 1 only).
 
 --impl reference runs the reference's CPU algorithm (the oracle port; the
 reference's own build needs Boost/GSL, absent on the GPU host) on a bounded
@@ -142,17 +144,19 @@ SERVE_NZ = 256
 SERVE_MAX_CUBE = 1 << 22  # floats: larger (pixels, L) draws are redrawn (16 MB host result cap)
 
 
-def serving_leg(device, n_req=300, rate=200.0, seed=11):
+def serving_leg(device, n_req=300, rates=(200.0, 400.0, 800.0), seed=11):
     """Mixed request stream through the continuous-batching server.
 
-    Eight resident flux-rope snapshots of 0.5M-8M points; Poisson arrivals at
-    `rate` per second (seeded); per request a random snapshot, view (l in
-    [0, 90 deg], b in [-20, 20 deg]), pixels in {64, 128, 256, 512, 1024}^2 and
-    L in {1, 16, 64, 128} (L = 1 renders one of six broadband DN channels,
-    otherwise one of four spectral lines), nz = 256.  Latency is submit ->
-    result in the caller's host buffer.  The same requests are then run alone,
-    one at a time, through the same server: their latency, their throughput,
-    and the largest difference between each cube alone and in the mix."""
+    Eight resident flux-rope snapshots of 0.5M-8M points; per request a random
+    snapshot, view (l in [0, 90 deg], b in [-20, 20 deg]), pixels in {64, 128,
+    256, 512, 1024}^2 and L in {1, 16, 64, 128} (L = 1 renders one of six
+    broadband DN channels, otherwise one of four spectral lines), nz = 256.
+    The requests are first run alone, one at a time, through the same server
+    (their latency and throughput), then as Poisson streams (seeded) at each
+    rate in `rates`: 200/s is the configured stream, the faster ones are above
+    what the server sustains running the requests one at a time.  Latency is
+    submit -> result in the caller's host buffer.  Every cube of every stream
+    is compared with the same request's cube alone."""
     import fomo_gb300 as fg
     from fomo_gb300 import synth
     rng = np.random.default_rng(seed)
@@ -171,7 +175,7 @@ def serving_leg(device, n_req=300, rate=200.0, seed=11):
             tid = band_t[int(rng.integers(len(band_t)))] if L == 1 else line_t[int(rng.integers(len(line_t)))]
             reqs.append(ctx.request(sid, tid, fg.METHOD_NN, npx, npx, SERVE_NZ, L, float(rng.uniform(0, math.pi / 2)),
                                     float(rng.uniform(-math.pi / 9, math.pi / 9)), WIDTH))
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+        unit_arrivals = np.cumsum(rng.exponential(1.0, n_req))  # Poisson at 1/s, scaled per rate
         # warm-up: every (snapshot, table) pair's emissivity, computed once and kept resident
         pairs = sorted({(q.snapshot, q.table, q.nlambda == 1) for q in reqs})
         for sid, tid, img in pairs:
@@ -179,36 +183,51 @@ def serving_leg(device, n_req=300, rate=200.0, seed=11):
             buf = np.empty(8 * 8 * q.nlambda, np.float32)
             srv.wait(srv.submit(q, buf))
         elems = [q.nx * q.ny * q.nlambda for q in reqs]
-        outs = [np.empty(e, np.float32) for e in elems]
-        t0 = time.perf_counter()
-        tickets = []
-        for i, q in enumerate(reqs):
-            delay = arrivals[i] - (time.perf_counter() - t0)
-            if delay > 0:
-                time.sleep(delay)
-            tickets.append(srv.submit(q, outs[i]))
-        st = [srv.wait(t, timeout=900.0) for t in tickets]
-        lat = np.array([s.t_done - s.t_submit for s in st]) * 1e3
-        span = max(s.t_done for s in st) - min(s.t_submit for s in st)
         samples = float(sum(q.nx * q.ny * q.nz for q in reqs))
-        # the same requests alone, one at a time
-        alone_lat, worst = [], 0.0
+        # the requests alone, one at a time
+        alone, alone_lat = [], []
         t1 = time.perf_counter()
         for i, q in enumerate(reqs):
             a = np.empty(elems[i], np.float32)
             s = srv.wait(srv.submit(q, a), timeout=900.0)
             alone_lat.append((s.t_done - s.t_submit) * 1e3)
-            den = float(np.abs(a).max())
-            if den > 0:
-                worst = max(worst, float(np.abs(a - outs[i]).max()) / den)
+            alone.append(a)
         alone_s = time.perf_counter() - t1
-    return {"requests": n_req, "arrival_rate_hz": rate, "arrivals": "Poisson, seeded",
-            "p50_ms": float(np.percentile(lat, 50)), "p90_ms": float(np.percentile(lat, 90)),
-            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()), "span_s": float(span),
-            "line_samples_per_s": samples / span,
+        outs = [np.empty(e, np.float32) for e in elems]
+        streams = []
+        for rate in rates:
+            arrivals = unit_arrivals / rate
+            t0 = time.perf_counter()
+            tickets = []
+            for i, q in enumerate(reqs):
+                delay = arrivals[i] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(q, outs[i]))
+            st = [srv.wait(t, timeout=900.0) for t in tickets]
+            lat = np.array([s.t_done - s.t_submit for s in st]) * 1e3
+            span = max(s.t_done for s in st) - min(s.t_submit for s in st)
+            worst, equal = 0.0, True
+            for a, o in zip(alone, outs):
+                equal = equal and np.array_equal(a, o)
+                den = float(np.abs(a).max())
+                if den > 0:
+                    worst = max(worst, float(np.abs(a - o).max()) / den)
+            streams.append({"arrival_rate_hz": rate, "p50_ms": float(np.percentile(lat, 50)),
+                            "p90_ms": float(np.percentile(lat, 90)), "p99_ms": float(np.percentile(lat, 99)),
+                            "mean_ms": float(lat.mean()), "span_s": float(span),
+                            "line_samples_per_s": samples / span,
+                            "vs_alone_throughput": (samples / span) / (samples / alone_s),
+                            "mix_vs_alone_max_norm_err": worst, "mix_bit_equal_alone": bool(equal)})
+    head = streams[0]
+    return {"requests": n_req, "arrival_rate_hz": head["arrival_rate_hz"], "arrivals": "Poisson, seeded",
+            "p50_ms": head["p50_ms"], "p90_ms": head["p90_ms"], "p99_ms": head["p99_ms"], "mean_ms": head["mean_ms"],
+            "span_s": head["span_s"], "line_samples_per_s": head["line_samples_per_s"],
             "alone_p50_ms": float(np.percentile(alone_lat, 50)), "alone_p99_ms": float(np.percentile(alone_lat, 99)),
-            "alone_line_samples_per_s": samples / alone_s, "mix_vs_alone_max_norm_err": worst,
-            "snapshots_points": list(SERVE_SNAPSHOT_POINTS), "nz": SERVE_NZ,
+            "alone_line_samples_per_s": samples / alone_s,
+            "mix_vs_alone_max_norm_err": max(s["mix_vs_alone_max_norm_err"] for s in streams),
+            "mix_bit_equal_alone": all(s["mix_bit_equal_alone"] for s in streams),
+            "streams": streams, "snapshots_points": list(SERVE_SNAPSHOT_POINTS), "nz": SERVE_NZ,
             "mix": "pixels {64..1024}^2 x L {1,16,64,128} (cube <= 16 MB), 4 lines / 6 DN channels, random views"}
 
 
@@ -339,6 +358,24 @@ def run_ours(args):
     line_samples = float(NVIEWS * len(tables) * NX * NY * NZ)
     value = world * line_samples * args.steps / t_total
 
+    # ---- the same 256 requests (64 views x 4 lines), one fomo_render_device call
+    # each: batched vs plain on identical work
+    torch.cuda.synchronize(dev)
+    for q, p in zip(reqs[:8], ptrs[:8]):
+        ctx.render_device(q, p, stream=sh)
+    torch.cuda.synchronize(dev)
+    same_ms = []
+    for k in range(2):
+        flush.fill_(5 + k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for q, p in zip(reqs, ptrs):
+            ctx.render_device(q, p, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        same_ms.append(e0.elapsed_time(e1))
+    plain_same_value = line_samples / (min(same_ms) / 1e3)
+
     # ---- plain single-request GPU render (denominator)
     from fomo_gb300 import synth
     t171 = ctx.table(synth.line_table())
@@ -418,6 +455,10 @@ def run_ours(args):
             "los_samples_per_step": NVIEWS * NX * NY * NZ,
             "plain_value": plain_value, "plain_unit": "LOS samples/s",
             "batched_vs_plain": value / plain_value,
+            "plain_same_config_value": plain_same_value, "plain_same_config_unit": "line-samples/s",
+            "plain_same_config": "the same 256 requests (64 views x 4 lines), one fomo_render_device call each, "
+                                 "L2 flushed before the 256 calls, CUDA events (best of 2)",
+            "batched_vs_plain_same_config": value / plain_same_value,
             "march_ms": float(np.mean(march_ms)), "march_timing": march_src,
             "e2e": {"value": e2e_value, "unit": "line-samples/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": len(e2e_times), "stat": "median",

@@ -106,7 +106,7 @@ struct MarchArgs {
   uint2* hard;                   // deferred samples (work item, sample) for a whole warp each, or null
   int64_t hard_cap;              // its capacity (0: every deferred sample is searched by one lane)
   int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
-  int32_t* npos;                 // spectral two-pass march: neighbour per (work item - item_base, sample), or null
+  int32_t* npos;                 // neighbour per (work item - item_base, sample), or null (the fused no-allocation march)
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
   unsigned int* err;             // device error word (bounds-check builds)

@@ -2,13 +2,16 @@
 // fomo-thomson.cpp:268-343), one warp per ray, persistent over a queue of
 // (view, ray) work items so that many views and requests share one launch.
 //
-// Kernels, in stream order: the first pass (march_search for spectral renders,
-// which stores each sample's neighbour in a buffer, then
-// march_spectral<.., shade> which bins the emission from it; march_imaging for
-// imaging and Thomson, which does both; march_spectral<.., fused> on the
-// no-allocation path), march_split (segments whose capsule overflowed),
-// march_deferred (samples the first pass could not resolve, one lane each)
-// and march_hard (deferred samples over a lane's budget, one warp each).
+// Kernels, in stream order: march_search (stores each sample's neighbour in a
+// position buffer), march_split (segments whose capsule overflowed),
+// march_deferred (samples the search could not resolve, one lane each),
+// march_hard (deferred samples over a lane's budget, one warp each) -- the
+// last three store the neighbours they find in the same buffer -- and then the
+// emission pass, march_spectral<.., shade> or march_imaging<.., shade>, which
+// bins every ray from the buffer.  The no-allocation path has no buffer: its
+// first pass (march_spectral / march_imaging, fused) searches and bins, and
+// the split, deferred and hard passes add their samples' emission with
+// atomics.
 //
 // Per ray: the FP64 per-ray terms of the derotation (x cos b cos l + y sin l,
 // -x cos b sin l + y cos l, -x sin b) are formed once; each LOS sample adds the
@@ -54,9 +57,9 @@
 // Gaussian can exceed 2^-64 of its peak; the others are written as 0) in a
 // per-chunk FP32 partial, folded into the per-ray sum with Kahan compensation.
 // Imaging (L = 1) and Thomson (pB) add per-sample values through a warp
-// reduction.  One warp owns one ray in the first pass and in the emission pass
-// (no atomics); the deferred samples' emission is added with atomics
-// afterwards.
+// reduction.  One warp owns one ray in the emission pass, which sums its
+// samples in order (no atomics), so a cube does not depend on what else
+// shares the launch.
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
@@ -1006,15 +1009,19 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
 // ---------------------------------------------------------------------------
 // Imaging (L == 1, broadband channels) and Thomson pB: per-sample values,
 // reduced across the warp per 32-sample chunk, Kahan-accumulated per ray.
+// SHADE: the neighbours come from the position buffer (a.npos), in which the
+// search, split, deferred and hard passes have stored every sample's
+// neighbour; otherwise (the no-allocation path) the kernel searches itself and
+// the deferred samples are added by the later passes.
 // ---------------------------------------------------------------------------
-template <int NL, bool THOMSON>
-__global__ void __launch_bounds__(kThreads, kMinCtasImaging) march_imaging(MarchArgs a, const double3* __restrict__ ktab,
-                                                          int ktab_stride) {
-  __shared__ SegSmem segs[kWarps];
-  SegSmem& sm = segs[threadIdx.x >> 5];
+template <int NL, bool THOMSON, bool SHADE>
+__global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtasImaging)
+    march_imaging(MarchArgs a, const double3* __restrict__ ktab, int ktab_stride) {
+  __shared__ SegSmem segs[SHADE ? 1 : kWarps];
+  SegSmem& sm = segs[SHADE ? 0 : (threadIdx.x >> 5)];
   const int lane = threadIdx.x & 31;
   RayCtx r;
-  while (next_ray(a, ktab, ktab_stride, r)) {
+  while (next_ray(a, ktab, ktab_stride, r, SHADE ? kCtrShade : kCtrRays)) {
     const ViewDesc* V = a.views + r.v;
     const int nz = V->nz, nx = V->nx;
     const LineDesc* LD = a.lines + (int64_t)r.v * a.nlines;
@@ -1027,11 +1034,17 @@ __global__ void __launch_bounds__(kThreads, kMinCtasImaging) march_imaging(March
       lon[l] = l < a.nlines && LD[l].out != nullptr;  // views may have fewer lines than the launch
     }
     const float* s2v = THOMSON ? a.s2 + (int64_t)r.v * a.snap.n : nullptr;
-    int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
+    int32_t* nnout = (!SHADE && a.nn_idx) ? a.nn_idx[r.v] : nullptr;
     const int64_t ray = (int64_t)r.i * nx + r.j;
+    const int32_t* npos = SHADE ? a.npos + ((int64_t)r.item - a.item_base) * ktab_stride : nullptr;
     for (int s0 = 0; s0 < nz; s0 += kSeg) {
       int posv[2], origv[2];
-      segment_search(a, r, s0, nz, sm, posv, origv);
+      if (SHADE) {
+        posv[0] = s0 + lane < nz ? __ldcs(npos + s0 + lane) : -1;
+        posv[1] = s0 + 32 + lane < nz ? __ldcs(npos + s0 + 32 + lane) : -1;
+      } else {
+        segment_search(a, r, s0, nz, sm, posv, origv);
+      }
 #pragma unroll 1
       for (int h = 0; h < 2; ++h) {
         const int k = s0 + 32 * h + lane;
@@ -1476,13 +1489,26 @@ __device__ __forceinline__ DeferredRec deferred_at(const MarchArgs& a, int64_t n
   return ri < nback ? a.deferred[a.deferred_cap - 1 - ri] : a.deferred[ri - nback];
 }
 
-// A deferred sample's result: its NN index, and its neighbour and LOS speed
-// staged for the emission step.
+// Sample k of work item `item` in the position buffer (rows of `stride`
+// entries from the launch's first work item).
+__device__ __forceinline__ int32_t* npos_at(const MarchArgs& a, unsigned item, int k, int stride) {
+  return a.npos + ((int64_t)item - a.item_base) * stride + k;
+}
+
+// A deferred sample's result: its NN index, and its neighbour -- into the
+// position buffer (POS: the emission pass bins it later, in sample order), or
+// staged with its LOS speed for this kernel's own emission step (the
+// no-allocation path).
+template <bool POS>
 __device__ __forceinline__ void store_deferred(const MarchArgs& a, const RayCtx& r, int k, int kind, int p, int o,
-                                               int* sp, float* sv) {
+                                               int stride, int* sp, float* sv) {
   const ViewDesc* V = a.views + r.v;
   int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
   if (nnout) nnout[((int64_t)r.i * V->nx + r.j) * V->nz + k] = o;
+  if (POS) {
+    *npos_at(a, r.item, k, stride) = p;
+    return;
+  }
   float vl = 0.0f;
   if (p >= 0 && kind == kDeferredSpectral) {
     const float4 vv = __ldg(a.snap.vel + p);
@@ -1497,15 +1523,16 @@ __device__ __forceinline__ void store_deferred(const MarchArgs& a, const RayCtx&
 // (dense clumps, long segments at a coarse LOS step) is queued by the first
 // pass at the back of the deferred buffer with all its samples.  This kernel
 // searches each such segment again as parts of 32 samples (16 when a part
-// overflows too), each part gathering its own, shorter capsule, adds the
-// emission of the samples it resolves and rewrites the record with the
-// samples still unresolved, for march_deferred.
+// overflows too), each part gathering its own, shorter capsule, stores the
+// neighbours of the samples it resolves (POS) or adds their emission, and
+// rewrites the record with the samples still unresolved, for march_deferred.
 // ---------------------------------------------------------------------------
+template <bool POS>
 __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs a, const double3* __restrict__ ktab,
                                                         int ktab_stride, int kind) {
   __shared__ SegSmem segs[kWarps];
-  __shared__ int spos[kWarps][kSeg];
-  __shared__ float svlos[kWarps][kSeg];
+  __shared__ int spos[kWarps][POS ? 1 : kSeg];
+  __shared__ float svlos[kWarps][POS ? 1 : kSeg];
   const int w = threadIdx.x >> 5;
   SegSmem& sm = segs[w];
   const int lane = threadIdx.x & 31;
@@ -1541,6 +1568,10 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
     for (int i = 0; i < 2; ++i) {
       const bool done = in.act[i] && !o.need[i];
       if (nnout && done) nnout[ray * nz + s0 + lane + 32 * i] = o.orig[i];
+      if (POS) {
+        if (done) *npos_at(a, rec.x, s0 + lane + 32 * i, ktab_stride) = o.pos[i];
+        continue;
+      }
       const bool fill = done && o.pos[i] >= 0;
       const unsigned fm = __ballot_sync(kFull, fill);
       if (fill) {
@@ -1555,9 +1586,11 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
       }
       n += __popc(fm);
     }
-    __syncwarp();
-    if (n > 0) add_emission(a, r, kind, spos[w], svlos[w], n);
-    __syncwarp();  // the staging arrays are rewritten by the next record
+    if (!POS) {
+      __syncwarp();
+      if (n > 0) add_emission(a, r, kind, spos[w], svlos[w], n);
+      __syncwarp();  // the staging arrays are rewritten by the next record
+    }
     const unsigned f0 = __ballot_sync(kFull, in.act[0] && o.need[0]);
     const unsigned f1 = __ballot_sync(kFull, in.act[1] && o.need[1]);
     if (lane == 0) a.deferred[slot] = make_uint4(rec.x, rec.y, f0, f1);
@@ -1570,10 +1603,10 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
 // budget goes to the hard queue (a whole warp searches it in march_hard) and
 // adds nothing here.  A long queue has no budget: 32 lanes on 32 samples keep
 // more loads in flight than a warp on one, and its walk has no budget checks.
-template <bool BUDGET>
+template <bool BUDGET, bool POS>
 __device__ __forceinline__ void deferred_search(const MarchArgs& a, int kind, int nsamp, int start, int incl,
-                                                int excl, const DeferredRec& rec, const RayCtx& mine, int* sp,
-                                                float* sv) {
+                                                int excl, const DeferredRec& rec, const RayCtx& mine, int stride,
+                                                int* sp, float* sv) {
   const int lane = threadIdx.x & 31;
   for (int t0 = 0; t0 < nsamp; t0 += 32) {
     const int t = t0 + lane;
@@ -1607,19 +1640,27 @@ __device__ __forceinline__ void deferred_search(const MarchArgs& a, int kind, in
     }
     if (t < nsamp) {
       if (hard) {
-        sp[t] = -1;
-        sv[t] = 0.0f;
+        // its neighbour comes from march_hard (the position buffer keeps the
+        // search pass's -1 until then)
+        if (!POS) {
+          sp[t] = -1;
+          sv[t] = 0.0f;
+        }
       } else {
-        store_deferred(a, r, k, kind, p, o, sp + t, sv + t);
+        store_deferred<POS>(a, r, k, kind, p, o, stride, sp + t, sv + t);
       }
     }
   }
 }
 
+// POS: the neighbours go to the position buffer and the emission pass that
+// runs after this kernel bins them; otherwise (the no-allocation path) this
+// kernel adds their emission to the already written cube with atomics.
+template <bool POS>
 __global__ void __launch_bounds__(kThreads, kMinCtasDeferred) march_deferred(MarchArgs a, const double3* __restrict__ ktab,
                                                            int ktab_stride, int kind) {
-  __shared__ int spos[kWarps][kDefBatch];    // neighbour (sorted position) of each staged sample
-  __shared__ float svlos[kWarps][kDefBatch]; // and its LOS speed (spectral)
+  __shared__ int spos[kWarps][POS ? 1 : kDefBatch];    // neighbour (sorted position) of each staged sample
+  __shared__ float svlos[kWarps][POS ? 1 : kDefBatch]; // and its LOS speed (spectral)
   const int w = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   // written by the march and march_split; the two ends of the buffer never meet
@@ -1657,18 +1698,20 @@ __global__ void __launch_bounds__(kThreads, kMinCtasDeferred) march_deferred(Mar
       const int nsamp = __shfl_sync(kFull, incl, r1 - 1) - start;
       // 1. one sample per lane: its record, ray and box, then its own search
       if (budgeted)
-        deferred_search<true>(a, kind, nsamp, start, incl, excl, rec, mine, spos[w], svlos[w]);
+        deferred_search<true, POS>(a, kind, nsamp, start, incl, excl, rec, mine, ktab_stride, spos[w], svlos[w]);
       else
-        deferred_search<false>(a, kind, nsamp, start, incl, excl, rec, mine, spos[w], svlos[w]);
-      __syncwarp();
-      // 2. their emission, record by record
-      for (int rr = r0; rr < r1; ++rr) {
-        const int sn = __shfl_sync(kFull, cnt, rr);
-        const int so = __shfl_sync(kFull, excl, rr) - start;
-        const RayCtx r = shfl_ray(mine, rr);
-        if (sn > 0) add_emission(a, r, kind, spos[w] + so, svlos[w] + so, sn);
+        deferred_search<false, POS>(a, kind, nsamp, start, incl, excl, rec, mine, ktab_stride, spos[w], svlos[w]);
+      if (!POS) {
+        __syncwarp();
+        // 2. their emission, record by record
+        for (int rr = r0; rr < r1; ++rr) {
+          const int sn = __shfl_sync(kFull, cnt, rr);
+          const int so = __shfl_sync(kFull, excl, rr) - start;
+          const RayCtx r = shfl_ray(mine, rr);
+          if (sn > 0) add_emission(a, r, kind, spos[w] + so, svlos[w] + so, sn);
+        }
+        __syncwarp();  // the staging arrays are rewritten by the next batch
       }
-      __syncwarp();  // the staging arrays are rewritten by the next batch
       r0 = r1;
     }
   }
@@ -1679,8 +1722,10 @@ __global__ void __launch_bounds__(kThreads, kMinCtasDeferred) march_deferred(Mar
 // (dense cells, or a wide box reaching far from the points).  One warp per
 // sample, from a queue shared by the whole grid: the rows and points of each
 // ring are spread over the lanes (warp_search).  The warp writes the NN index
-// and adds the sample's emission with atomics.
+// and stores the neighbour in the position buffer (POS) or adds the sample's
+// emission with atomics.
 // ---------------------------------------------------------------------------
+template <bool POS>
 __global__ void __launch_bounds__(kThreads, kMinCtas) march_hard(MarchArgs a, const double3* __restrict__ ktab,
                                                        int ktab_stride, int kind) {
   __shared__ int sp[kWarps];
@@ -1698,10 +1743,12 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_hard(MarchArgs a, co
     if (!ray_of_item(a, ktab, ktab_stride, (int64_t)hs.x, r)) continue;  // queued from real rays only
     int p, o;
     warp_search(a.snap, exact_box(r, (int)hs.y), p, o);
-    if (lane == 0) store_deferred(a, r, (int)hs.y, kind, p, o, sp + w, sv + w);
-    __syncwarp();
-    if (p >= 0) add_emission(a, r, kind, sp + w, sv + w, 1);
-    __syncwarp();  // sp / sv are rewritten by the next sample
+    if (lane == 0) store_deferred<POS>(a, r, (int)hs.y, kind, p, o, ktab_stride, sp + w, sv + w);
+    if (!POS) {
+      __syncwarp();
+      if (p >= 0) add_emission(a, r, kind, sp + w, sv + w, 1);
+      __syncwarp();  // sp / sv are rewritten by the next sample
+    }
   }
 }
 
@@ -1721,69 +1768,61 @@ cudaError_t launch_persistent(K kernel, const MarchArgs& a, const double3* ktab,
   return cudaGetLastError();
 }
 
-cudaError_t launch_deferred(const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count, cudaStream_t s,
-                            int kind) {
+// A persistent grid over a queue whose length is known on the device only (it
+// drains the queue and exits at once when it is empty).
+template <typename K>
+cudaError_t launch_queue(K kernel, const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count,
+                         cudaStream_t s, int kind) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_deferred, kThreads, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
-  // the record count is known on the device only: a persistent grid that
-  // drains the queue (and exits at once when it is empty)
-  march_deferred<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
+  kernel<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
   return cudaGetLastError();
 }
 
-cudaError_t launch_hard(const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count, cudaStream_t s,
-                        int kind) {
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_hard, kThreads, 0);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) per_sm = 1;
-  march_hard<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_split(const MarchArgs& a, const double3* ktab, int ktab_stride, int sm_count, cudaStream_t s,
-                         int kind) {
-  int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_split, kThreads, 0);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) per_sm = 1;
-  march_split<<<(unsigned)(sm_count * per_sm), kThreads, 0, s>>>(a, ktab, ktab_stride, kind);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_first_pass(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows,
-                              int sm_count, cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
-  const bool thomson = a.s2 != nullptr;
-  if (thomson) return launch_persistent(march_imaging<1, true>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+// The kernel that bins the emission from the position buffer (after every
+// search pass has stored its neighbours).
+cudaError_t launch_emission_pass(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows,
+                                 int sm_count, cudaStream_t s, bool imaging) {
+  if (a.s2) return launch_persistent(march_imaging<1, true, true>, a, ktab, ktab_stride, sm_count, s, 0);
   if (imaging) {
-    if (a.nlines <= 1) return launch_persistent(march_imaging<1, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
-    if (a.nlines <= 2) return launch_persistent(march_imaging<2, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
-    if (a.nlines <= 4) return launch_persistent(march_imaging<4, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
-    if (a.nlines <= 8) return launch_persistent(march_imaging<8, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+    if (a.nlines <= 1) return launch_persistent(march_imaging<1, false, true>, a, ktab, ktab_stride, sm_count, s, 0);
+    if (a.nlines <= 2) return launch_persistent(march_imaging<2, false, true>, a, ktab, ktab_stride, sm_count, s, 0);
+    if (a.nlines <= 4) return launch_persistent(march_imaging<4, false, true>, a, ktab, ktab_stride, sm_count, s, 0);
+    if (a.nlines <= 8) return launch_persistent(march_imaging<8, false, true>, a, ktab, ktab_stride, sm_count, s, 0);
     return cudaErrorInvalidValue;
   }
   const int nb = max_windows < 1 ? 1 : max_windows;
-  if (a.npos) {
-    // two passes: the search, then the emission from the stored positions
-    cudaError_t e = launch_persistent(march_search, a, ktab, ktab_stride, sm_count, s, 0);
-    if (e != cudaSuccess) return e;
 #define FOMO_SHADE(NL_, NB_) \
   if (a.nlines <= NL_ && nb <= NB_) return launch_persistent(march_spectral<NL_, NB_, true>, a, ktab, ktab_stride, sm_count, s, 0)
-    FOMO_SHADE(1, 1);
-    FOMO_SHADE(1, 2);
-    FOMO_SHADE(1, 4);
-    FOMO_SHADE(1, 8);
-    FOMO_SHADE(2, 1);
-    FOMO_SHADE(2, 2);
-    FOMO_SHADE(2, 4);
-    FOMO_SHADE(4, 1);
-    FOMO_SHADE(4, 2);
-    FOMO_SHADE(4, 4);
+  FOMO_SHADE(1, 1);
+  FOMO_SHADE(1, 2);
+  FOMO_SHADE(1, 4);
+  FOMO_SHADE(1, 8);
+  FOMO_SHADE(2, 1);
+  FOMO_SHADE(2, 2);
+  FOMO_SHADE(2, 4);
+  FOMO_SHADE(4, 1);
+  FOMO_SHADE(4, 2);
+  FOMO_SHADE(4, 4);
 #undef FOMO_SHADE
+  return cudaErrorInvalidValue;
+}
+
+// The fused first pass of the no-allocation path: search and emission in one
+// kernel (no position buffer).
+cudaError_t launch_fused_pass(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows,
+                              int sm_count, cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
+  if (a.s2) return launch_persistent(march_imaging<1, true, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+  if (imaging) {
+    if (a.nlines <= 1) return launch_persistent(march_imaging<1, false, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+    if (a.nlines <= 2) return launch_persistent(march_imaging<2, false, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+    if (a.nlines <= 4) return launch_persistent(march_imaging<4, false, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+    if (a.nlines <= 8) return launch_persistent(march_imaging<8, false, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
     return cudaErrorInvalidValue;
   }
+  const int nb = max_windows < 1 ? 1 : max_windows;
 #define FOMO_SPEC(NL_, NB_) \
   if (a.nlines <= NL_ && nb <= NB_) return launch_persistent(march_spectral<NL_, NB_, false>, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint)
   FOMO_SPEC(1, 1);
@@ -1808,16 +1847,32 @@ int march_bins_per_lane(int nlines, int L) {
 }
 
 // max_windows: largest number of 32-bin lambda windows of any line (1 for imaging).
+//
+// With a position buffer (a.npos): the search stores every sample's neighbour,
+// the split, deferred and hard passes store the neighbours of the samples it
+// left, and the emission pass then bins every ray from the buffer in sample
+// order.  One warp owns one ray there and nothing is added with atomics, so a
+// cube is the same bits whatever else shares the launch.  Without one (the
+// no-allocation path): the fused first pass searches and bins, and the later
+// passes add the deferred samples' emission with atomics.
 cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
                          cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
   if (!a.deferred || a.deferred_cap <= 0 || !a.counter) return cudaErrorInvalidValue;
-  cudaError_t e = launch_first_pass(a, ktab, ktab_stride, max_windows, sm_count, s, blocks_per_sm_hint, imaging);
-  if (e != cudaSuccess) return e;
   const int kind = a.s2 ? kDeferredThomson : (imaging ? kDeferredImaging : kDeferredSpectral);
-  e = launch_split(a, ktab, ktab_stride, sm_count, s, kind);
-  if (e == cudaSuccess) e = launch_deferred(a, ktab, ktab_stride, sm_count, s, kind);
-  if (e != cudaSuccess || a.hard_cap <= 0) return e;
-  return launch_hard(a, ktab, ktab_stride, sm_count, s, kind);
+  cudaError_t e;
+  if (a.npos) {
+    e = launch_persistent(march_search, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+    if (e == cudaSuccess) e = launch_queue(march_split<true>, a, ktab, ktab_stride, sm_count, s, kind);
+    if (e == cudaSuccess) e = launch_queue(march_deferred<true>, a, ktab, ktab_stride, sm_count, s, kind);
+    if (e == cudaSuccess && a.hard_cap > 0) e = launch_queue(march_hard<true>, a, ktab, ktab_stride, sm_count, s, kind);
+    if (e == cudaSuccess) e = launch_emission_pass(a, ktab, ktab_stride, max_windows, sm_count, s, imaging);
+    return e;
+  }
+  e = launch_fused_pass(a, ktab, ktab_stride, max_windows, sm_count, s, blocks_per_sm_hint, imaging);
+  if (e == cudaSuccess) e = launch_queue(march_split<false>, a, ktab, ktab_stride, sm_count, s, kind);
+  if (e == cudaSuccess) e = launch_queue(march_deferred<false>, a, ktab, ktab_stride, sm_count, s, kind);
+  if (e == cudaSuccess && a.hard_cap > 0) e = launch_queue(march_hard<false>, a, ktab, ktab_stride, sm_count, s, kind);
+  return e;
 }
 
 }  // namespace fomo

@@ -8,10 +8,15 @@
 // batched forms) keep their per-render working memory in a context arena that
 // grows with cudaMalloc when a larger render comes along.  This entry point
 // instead places that working memory -- the view and line descriptors, the
-// lambda table, the per-sample derotation table, the per-ray position tables
-// the work counters and the deferred-sample queue (whose fixed capacity makes
-// a large render march its rays in chunks) -- in one file-scope static __device__ array of fixed
-// size, so a call never allocates.
+// lambda table, the per-sample derotation table, the per-ray position tables,
+// the work counters and the deferred-sample queue -- in one file-scope static
+// __device__ array of fixed size, so a call never allocates.  The descriptors
+// reach the array as the parameter of a small kernel, not through a host
+// copy.  The queue's fixed capacity (65,536 segment records) makes a large
+// render march its rays in chunks; each chunk costs a counter clear and four
+// launches (first pass, split, deferred and hard passes), so a render at the
+// limits (4096 x 4096 rays at nz = 4096: chunks of 1,024 rays) issues about
+// 16,000 chunks.
 //
 // The array costs every GPU that loads the library kNoAllocScratchBytes of
 // device memory until the process exits.  Its device address is looked up
@@ -24,7 +29,10 @@
 // array; serialise them.
 //
 // The kernels are the ones every other render uses (view set-up and the ray
-// march); only the place of their scratch differs.
+// march); only the place of their scratch differs.  With no room for a
+// neighbour buffer, the march is the fused one: the first pass searches and
+// bins, and the deferred samples' emission is added with atomics, so a cube
+// matches the regular render's to FP32 summation order (not bit for bit).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -60,6 +68,20 @@ constexpr size_t kNoAllocScratchBytes = align_up(kOffDeferred + (size_t)kNoAlloc
 
 // The scratch of fomo_render_noalloc (about 1.2 MB per device).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// The per-call descriptors (view, line, ray offsets, lambda table), built on
+// the host.  They travel to the scratch array as a kernel parameter: a kernel
+// argument is copied when the launch is issued, so the host buffer may go
+// away at once and nothing goes through pageable memory.
+struct HeaderBlob {
+  uint4 w[kHdrBytes / sizeof(uint4)];
+};
+static_assert(kHdrBytes % sizeof(uint4) == 0, "header size");
+static_assert(sizeof(HeaderBlob) <= 4000, "descriptors must fit the kernel parameter space");
+
+__global__ void put_header(const HeaderBlob blob, uint4* dst) {
+  for (int i = threadIdx.x; i < (int)(kHdrBytes / sizeof(uint4)); i += blockDim.x) dst[i] = blob.w[i];
+}
 
 constexpr int kMaxDevices = 64;
 std::mutex g_addr_mu;
@@ -110,9 +132,11 @@ extern "C" int fomo_render_noalloc(fomo_ctx* ctx, const fomo_request* req, float
 
   const SnapRec& snap = ctx->snaps[q.snapshot];
   const TableHost& t = ctx->tables[q.table].h;
-  // descriptors, built on the host and copied into the static array
-  alignas(16) unsigned char hdr[kHdrBytes];
-  std::memset(hdr, 0, sizeof(hdr));
+  // descriptors, built on the host and written into the static array by a
+  // kernel that receives them as its parameter
+  HeaderBlob blob;
+  unsigned char* hdr = reinterpret_cast<unsigned char*>(blob.w);
+  std::memset(hdr, 0, sizeof(blob));
   ViewDesc* hv = reinterpret_cast<ViewDesc*>(hdr + kOffView);
   LineDesc* hl = reinterpret_cast<LineDesc*>(hdr + kOffLine);
   int64_t* hoff = reinterpret_cast<int64_t*>(hdr + kOffRayOff);
@@ -139,7 +163,8 @@ extern "C" int fomo_render_noalloc(fomo_ctx* ctx, const fomo_request* req, float
   ViewDesc* dv = reinterpret_cast<ViewDesc*>(base + kOffView);
   double3* ktab = reinterpret_cast<double3*>(base + kOffKtab);
   unsigned long long* counter = reinterpret_cast<unsigned long long*>(base + kOffCounter);
-  e = cudaMemcpyAsync(base, hdr, kHdrBytes, cudaMemcpyHostToDevice, s);
+  put_header<<<1, 128, 0, s>>>(blob, reinterpret_cast<uint4*>(base));
+  e = cudaGetLastError();
   const SnapDev sd = snap_dev(snap);
   if (e == cudaSuccess) e = launch_view_init(dv, 1, s);
   if (e == cudaSuccess) e = launch_view_extents(sd, dv, 1, nullptr, s);

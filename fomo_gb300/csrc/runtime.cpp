@@ -737,13 +737,13 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     G.o_def = L.take(sizeof(DeferredRec) * (size_t)G.deferred_cap);
     G.hard_cap = hard_capacity(items, G.maxnz);
     G.o_hard = L.take(sizeof(uint2) * (size_t)G.hard_cap);
-    // spectral NN: the search and the emission run as two passes through a
-    // neighbour buffer
-    // (each pass at its own occupancy); at most ctx->npos_cap entries, the
-    // launch marching in item chunks beyond that
+    // the searches and the emission run as separate passes through a
+    // neighbour buffer (each pass at its own occupancy; the emission pass runs
+    // last, so no sample is added with atomics); at most ctx->npos_cap
+    // entries, the launch marching in item chunks beyond that
     G.npos_items = 0;
     G.o_npos = 0;
-    if (G.method == FOMO_METHOD_NN && !G.imaging) {
+    if (G.method != FOMO_METHOD_PROJECTION) {
       const int64_t cap_items = std::max<int64_t>(1, ctx->npos_cap / G.maxnz);
       G.npos_items = std::min<int64_t>(items, cap_items);
       G.o_npos = L.take(sizeof(int32_t) * (size_t)G.npos_items * G.maxnz);

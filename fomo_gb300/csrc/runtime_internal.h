@@ -101,7 +101,7 @@ struct PlanGroup {
   int64_t deferred_cap = 0;  // records: one per segment of every work item
   size_t o_hard = 0;
   int64_t hard_cap = 0;      // hard-sample queue entries
-  size_t o_npos = 0;         // spectral two-pass march: a neighbour per (work item, sample), or 0
+  size_t o_npos = 0;         // a neighbour per (work item, sample) for the emission pass, or 0 (projection)
   int64_t npos_items = 0;    // work items the neighbour buffer holds (the launch marches in chunks of these)
   std::vector<int64_t> item_off;  // first work item of each view (nv + 1 entries)
   std::vector<double> vcost;      // LOS samples + output cells of each view

@@ -107,7 +107,7 @@ size_t request_cost(const fomo_request& q) {
   return cube_elems(q) * sizeof(float) + (size_t)q.nz * 24 + (size_t)(q.nx + q.ny) * 8 + 64 * 1024 +
          rays * (size_t)((q.nz + 63) / 64) * sizeof(DeferredRec) +
          (size_t)hard_capacity((int64_t)rays, q.nz) * sizeof(uint2) +
-         (q.nlambda > 1 ? rays * (size_t)q.nz * sizeof(int32_t) : 0);  // neighbour buffer of the spectral march
+         (q.method != FOMO_METHOD_PROJECTION ? rays * (size_t)q.nz * sizeof(int32_t) : 0);  // neighbour buffer
 }
 
 // Requests `ids` of slot sl are complete (their cubes are in pinned staging);

@@ -189,14 +189,16 @@ int fomo_render_device(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube
  * that owns a fixed device-memory pool and forbids allocation in its frame
  * loop, or a real-time path where cudaMalloc/cudaFree would synchronise the
  * device).  The per-render working memory lives in one static device array of
- * about 167 KB that every GPU loading this library holds until exit; hence the
+ * about 1.2 MB that every GPU loading this library holds until exit; hence the
  * limits nz <= 4096, nx + ny <= 8192, nlambda <= 256 (larger requests return
  * FOMO_EINVAL).  The snapshot, the table and the emissivity of the pair must
  * already be resident (call fomo_emission or any regular render once first).
  * The first call on a device looks up the array's address, so make it before
  * any stream capture.  All calls share the array: calls that overlap on the
- * GPU (different streams) race and must be serialised.  Asynchronous on
- * `stream` (NULL = the context's stream). */
+ * GPU (different streams) race and must be serialised.  The cube matches
+ * fomo_render's to FP32 summation order (the deferred samples' emission is
+ * added with atomics here).  Asynchronous on `stream` (NULL = the context's
+ * stream). */
 int fomo_render_noalloc(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube, void* stream);
 
 /* Batched render: many views / lines / requests in one persistent launch.

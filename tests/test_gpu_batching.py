@@ -76,16 +76,17 @@ def test_host_batch_downloads_in_chunks_same_as_alone(ctx):
     cubes, infos = ctx.render_batch(reqs)
     for q, c, inf in zip(reqs, cubes, infos):
         single, _, sinf = ctx.render(q)
-        assert G.norm_max_err(c.ravel(), single.ravel()) <= 1e-6
+        np.testing.assert_array_equal(c, single)
         assert inf.as_dict() == sinf.as_dict()
     ctx.drop_snapshot(sid)
 
 
 def test_small_neighbour_buffer_marches_in_item_chunks(monkeypatch):
-    """FOMO_NPOS_CAP bounds the spectral march's neighbour buffer; a launch then
-    marches in chunks of work items.  Neighbour indices must equal those of an
-    unchunked render, and cubes must match up to the order of the deferred
-    passes' atomic additions; a host batch (view ranges + chunks) as well."""
+    """FOMO_NPOS_CAP bounds the march's neighbour buffer; a launch then marches
+    in chunks of work items.  Neighbour indices and cubes must be the same bits
+    as those of an unchunked render (the emission pass bins every ray from the
+    buffer in sample order, with no atomics); a host batch (view ranges +
+    chunks) as well."""
     s = synth.loop_snapshot(24, seed=5)
     t = synth.line_table()
     width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
@@ -105,10 +106,10 @@ def test_small_neighbour_buffer_marches_in_item_chunks(monkeypatch):
     with fg.Context(0) as c2:
         got = run(c2)
     np.testing.assert_array_equal(got[1], ref[1])
-    assert G.norm_max_err(got[0].ravel(), ref[0].ravel()) <= 1e-6
+    np.testing.assert_array_equal(got[0], ref[0])
     assert got[2].as_dict() == ref[2].as_dict()
     for a, b, ia, ib in zip(got[3], ref[3], got[4], ref[4]):
-        assert G.norm_max_err(a.ravel(), b.ravel()) <= 1e-6
+        np.testing.assert_array_equal(a, b)
         assert ia.as_dict() == ib.as_dict()
 
 
@@ -176,29 +177,6 @@ def test_unknown_ids_and_bad_arguments(ctx):
     with pytest.raises(fg.FomoError) as ei:
         ctx.load_table("/nonexistent/table.dat")
     assert ei.value.code == fg.EIO
-    ctx.drop_snapshot(sid)
-
-
-def test_full_size_plain_config_sampled_rows(ctx):
-    """128^3 = 2,097,152 points, 512x512 pixels, 128 bins, 512 samples, l = 30 deg:
-    neighbour indices of sampled image rows bit-exact, their spectra within 1e-4."""
-    s = synth.loop_snapshot(128, seed=1)
-    t = synth.line_table()
-    sid = ctx.snapshot(s)
-    tid = ctx.table(t)
-    width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
-    l = math.radians(30.0)
-    req = ctx.request(sid, tid, fg.METHOD_NN, 512, 512, 512, 128, l, 0.0, width)
-    cube, idx, info = ctx.render(req, want_idx=True)
-    eps, w = oracle.emission(s, t)
-    for r0 in (3, 255, 509):
-        oc, oi, ov = oracle.nn_render(s, eps, w, t.lambda0, l, 0.0, 512, 512, 512, 128, width, rows=(r0, r0 + 2),
-                                      want_idx=True)
-        np.testing.assert_array_equal(idx[r0:r0 + 2], oi)
-        assert info.maxdistance == ov[oracle.V_MAXDIST]
-        if np.abs(oc).max() > 0:
-            assert G.norm_max_err(cube[r0:r0 + 2].ravel(), oc.ravel()) <= 1e-4
-    assert (idx >= 0).mean() > 0.5
     ctx.drop_snapshot(sid)
 
 

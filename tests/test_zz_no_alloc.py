@@ -73,3 +73,34 @@ def test_noalloc_one_lane_searches_match_warp_searches_on_dense_cells():
             assert rc == fg.OK, lib.fomo_last_error(ctx.h).decode()
             ctx.synchronize()
             assert G.norm_max_err(out.cpu().numpy(), ref) <= 1e-5
+
+
+@pytest.mark.parametrize("nx,ny,nz,nlam", [(256, 256, 512, 32), (64, 64, 4096, 16)])
+def test_noalloc_render_in_several_chunks_matches_regular_render(nx, ny, nz, nlam):
+    """The static deferred-sample queue holds 65,536 segment records (one per 64
+    LOS samples of a ray), so a render with more segments marches its rays in
+    chunks: 65,536 rays x 8 segments in 8 chunks, and 4,096 rays x 64 segments
+    in 4 chunks of 1,024 rays.  Each chunk clears the work counters and starts
+    its rays from its own first work item; the cube must still match the
+    regular render's, on two calls in a row."""
+    import torch
+
+    with fg.Context(0) as ctx:
+        lib = fg.lib()
+        s = synth.loop_snapshot(32, seed=4)
+        t = synth.line_table()
+        sid = ctx.snapshot(s)
+        tid = ctx.table(t)
+        width = 0.6 * fg.SPEED_OF_LIGHT / t.lambda0
+        req = ctx.request(sid, tid, fg.METHOD_NN, nx, ny, nz, nlam, 0.45, 0.3, width)
+        ref, _, _ = ctx.render(req)
+        out = torch.empty(ref.shape, dtype=torch.float32, device="cuda:0")
+        for _ in range(2):
+            out.fill_(float("nan"))
+            torch.cuda.synchronize()
+            rc = lib.fomo_render_noalloc(ctx.h, ctypes.byref(req), ctypes.c_void_p(out.data_ptr()), None)
+            assert rc == fg.OK, lib.fomo_last_error(ctx.h).decode()
+            ctx.synchronize()
+            got = out.cpu().numpy()
+            assert np.isfinite(got).all()
+            assert G.norm_max_err(got, ref) <= TOL
