@@ -132,6 +132,54 @@ def make_workload(seed=1):
     return snap, tables, ls, bs
 
 
+def kernel_bounds(kernel_ms, counters, ceilings, clocks, samples):
+    """Each march kernel of the batch against the ceiling that binds it.
+
+    march_search: instruction issue -- warp instructions per LOS sample (the
+    committed ncu figure, profiles/march_ceilings.json) x samples / its time,
+    against 4 warp instructions per clock per SM at the sampled SM clock; and
+    its point loads (16 B each, counted) against the measured L2 gather rate.
+    Emission pass: the SFU -- ex2 evaluations (counted) / its time against the
+    measured ex2 throughput.  Deferred / split / hard: their time and share."""
+    total = sum(kernel_ms.values()) or 1.0
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    issue_peak = 4.0 * ceilings["sm_count"] * mhz * 1e6  # warp instructions per second
+    ipc = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "march_ceilings.json")) as f:
+            ipc = json.load(f)
+    except Exception:
+        ipc = None
+    out = {}
+    for name, ms in kernel_ms.items():
+        if ms <= 0.0:
+            continue
+        out[name] = {"ms": ms, "share": ms / total}
+    s = out.get("search")
+    if s:
+        sec = s["ms"] / 1e3
+        s["samples_per_s"] = samples / sec
+        per = (ipc or {}).get("march_search", {}).get("warp_inst_per_sample")
+        if per:
+            s["issue"] = {"achieved": per * samples / sec, "peak": issue_peak, "frac": per * samples / sec / issue_peak,
+                          "unit": "warp instructions/s", "per_sample": per}
+        gb = counters.get("points_loaded", 0) * 16.0 / sec / 1e9
+        s["l2_gather"] = {"achieved": gb, "peak": ceilings["l2_gather_gbs"], "frac": gb / ceilings["l2_gather_gbs"],
+                          "unit": "GB/s"}
+        s["bound"] = "issue"
+    e = out.get("emission")
+    if e and counters.get("ex2"):
+        rate = counters["ex2"] / (e["ms"] / 1e3)
+        e["sfu"] = {"achieved": rate, "peak": ceilings["ex2_per_s"], "frac": rate / ceilings["ex2_per_s"],
+                    "unit": "ex2/s", "runs": counters.get("runs")}
+        e["bound"] = "sfu"
+    for k in ("deferred", "split", "hard"):
+        if k in out:
+            out[k]["bound"] = "latency (dependent L2 loads per ring)"
+    out["counters"] = {k: v for k, v in counters.items() if v}
+    return out
+
+
 def algorithmic_bytes_per_sample(nlines, L, nz):
     # winning point's FP32 position (12 B) + v_los (4 B) + (eps, w) per line (8 B)
     # + the output cube written once per ray, spread over its LOS samples
@@ -358,6 +406,19 @@ def run_ours(args):
     line_samples = float(NVIEWS * len(tables) * NX * NY * NZ)
     value = world * line_samples * args.steps / t_total
 
+    # ---- the batch's kernels one by one: a direct launch of the same batch with
+    # events between the march's kernels, then one with the search counters on
+    # (they add atomics, so their run is not timed); then the device's ceilings
+    ctx.set_profiling(kernel_timing=True, counters=False)
+    flush.fill_(7)
+    ctx.render_batch_device(reqs, ptrs, stream=sh, graph=False)
+    kernel_ms, _ = ctx.profile_read()
+    ctx.set_profiling(kernel_timing=False, counters=True)
+    ctx.render_batch_device(reqs, ptrs, stream=sh, graph=False)
+    _, counters = ctx.profile_read()
+    ctx.set_profiling(kernel_timing=False, counters=False)
+    ceilings = ctx.measure_ceilings().as_dict()
+
     # ---- the same 256 requests (64 views x 4 lines), one fomo_render_device call
     # each: batched vs plain on identical work
     torch.cuda.synchronize(dev)
@@ -435,6 +496,9 @@ def run_ours(args):
         except Exception:
             traffic = None
 
+    clocks = clk.summary()
+    kernels = kernel_bounds(kernel_ms, counters, ceilings, clocks, samples_per_launch)
+
     serving = None
     if rank == 0 and world == 1 and not args.no_serving:
         ctx.close()  # the server leg builds its own context and snapshots
@@ -472,7 +536,9 @@ def run_ours(args):
                                    "(overflowing segments) + march_deferred (the samples the search leaves) + "
                                    "march_hard (deferred samples over the one-lane budget), timed together"},
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clocks,
+            "ceilings": ceilings,
+            "kernels": kernels,
             # per step: view init, view extents, view finalize, search, emission, overflow split, deferred march,
             # hard-sample march
             "gpu_launches": 8 * args.steps,
@@ -502,7 +568,9 @@ def ctx_snapshot_from_pinned(ctx, hsnap):
 
 def run_profile_case(args):
     """Small case for ncu: the batched workload cut to 8 views (268 M LOS samples,
-    ~130 MB resident), issued directly (no graph), 1 warm-up + 2 launches."""
+    ~130 MB resident), issued directly (no graph), 1 warm-up + 2 launches; then
+    (outside any ncu kernel filter of interest) one launch with per-kernel
+    events and one with the search counters, printed as JSON."""
     import fomo_gb300 as fg
     snap, tables, ls, bs = make_workload()
     with fg.Context(0) as ctx:
@@ -519,8 +587,18 @@ def run_profile_case(args):
             ctx.render_batch_device(reqs, ptrs)
             ms = ctx.last_march_ms()
         ctx.synchronize()
+        kernel_ms, counters = None, None
+        if not args.no_breakdown:
+            ctx.set_profiling(kernel_timing=True, counters=False)
+            ctx.render_batch_device(reqs, ptrs)
+            kernel_ms, _ = ctx.profile_read()
+            ctx.set_profiling(kernel_timing=False, counters=True)
+            ctx.render_batch_device(reqs, ptrs)
+            _, counters = ctx.profile_read()
+            ctx.set_profiling(False, False)
         print(json.dumps({"profile_case": f"{nv} views x {len(tables)} lines, {NX}x{NY}x{NZ}, L={NL}",
-                          "march_ms": ms, "los_samples": nv * NX * NY * NZ}))
+                          "march_ms": ms, "los_samples": nv * NX * NY * NZ, "kernel_ms": kernel_ms,
+                          "counters": counters}))
 
 
 def main():
@@ -532,6 +610,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (mixed request stream) leg")
     ap.add_argument("--profile-case", action="store_true", help="small direct-launch case for ncu captures")
+    ap.add_argument("--no-breakdown", action="store_true", help="profile case without the timing/counter launches")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

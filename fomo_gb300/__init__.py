@@ -26,6 +26,10 @@ METHOD_PROJECTION = 2
 OBS_SPECTROSCOPIC = 1
 OBS_IMAGING = 2
 SPEED_OF_LIGHT = 2.99792458e8
+# FOMO_KERNEL_* and FOMO_COUNTER_* of include/fomo_gpu.h, in order
+KERNELS = ("search", "split", "deferred", "hard", "emission", "fused")
+COUNTERS = ("segments", "candidates", "rows", "points_loaded", "not_gathered", "fallbacks", "samples", "scanned",
+            "ties", "fb_nocand", "fb_far", "fb_ambiguous", "deferred", "deferred_recs", "hard", "runs", "ex2")
 
 
 class FomoError(RuntimeError):
@@ -59,6 +63,14 @@ class SnapshotInfo(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t), ("max_inflight", ctypes.c_int)]
+
+
+class Ceilings(ctypes.Structure):
+    _fields_ = [("l2_read_gbs", ctypes.c_double), ("l2_gather_gbs", ctypes.c_double), ("ex2_per_s", ctypes.c_double),
+                ("sm_count", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class RequestStats(ctypes.Structure):
@@ -109,6 +121,10 @@ SIGNATURES = {
     "fomo_autotune": [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.c_int, ctypes.c_char_p],
     "fomo_set_march_config": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "fomo_last_march_ms": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)],
+    "fomo_measure_ceilings": [ctypes.c_void_p, ctypes.POINTER(Ceilings)],
+    "fomo_set_profiling": [ctypes.c_void_p, ctypes.c_int, ctypes.c_int],
+    "fomo_profile_read": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                          ctypes.POINTER(ctypes.c_uint64), ctypes.c_int],
     "fomo_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)],
     "fomo_server_context": [ctypes.c_void_p],
     "fomo_server_submit": [ctypes.c_void_p, ctypes.POINTER(Request), _F, ctypes.POINTER(ctypes.c_uint64)],
@@ -297,6 +313,23 @@ class Context:
         ms = ctypes.c_float()
         self._check(self._L.fomo_last_march_ms(self.h, ctypes.byref(ms)))
         return ms.value
+
+    def set_profiling(self, kernel_timing=True, counters=False):
+        """Per-kernel event times and/or search counters of later direct renders."""
+        self._check(self._L.fomo_set_profiling(self.h, int(kernel_timing), int(counters)))
+
+    def profile_read(self):
+        """({kernel: ms} of the last direct render, {counter: value} since the last read)."""
+        ms = (ctypes.c_float * len(KERNELS))()
+        cnt = (ctypes.c_uint64 * len(COUNTERS))()
+        self._check(self._L.fomo_profile_read(self.h, ms, len(KERNELS), cnt, len(COUNTERS)))
+        return dict(zip(KERNELS, list(ms))), dict(zip(COUNTERS, list(cnt)))
+
+    def measure_ceilings(self) -> Ceilings:
+        """L2 read and gather bandwidth and SFU ex2 throughput of this device."""
+        c = Ceilings()
+        self._check(self._L.fomo_measure_ceilings(self.h, ctypes.byref(c)))
+        return c
 
     def register_host(self, arr: np.ndarray):
         self._check(self._L.fomo_host_register(self.h, arr.ctypes.data, arr.nbytes))

@@ -110,7 +110,7 @@ struct MarchArgs {
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
   unsigned int* err;             // device error word (bounds-check builds)
-  unsigned long long* stats;     // optional search counters (FOMO_MARCH_STATS=1), else null
+  unsigned long long* stats;     // optional search counters (profiling), else null
 };
 
 // Search counters accumulated when MarchArgs::stats is set.
@@ -130,7 +130,25 @@ enum MarchStat {
   kStatFbUnion,        // samples searched by the deferred pass
   kStatDeferredRecs,   // deferred-sample records (segments with fallback samples)
   kStatHard,           // deferred samples whose one-lane search ran out of budget (searched by a warp)
+  kStatRuns,           // runs of equal neighbours binned by the spectral emission pass (with a neighbour)
+  kStatEx2,            // ex2 evaluations of the spectral emission pass (32 per run, line and 32-bin window)
   kStatCount
+};
+
+// Kernels of one march, for optional per-kernel timing (direct launches
+// only): events recorded on the stream after each kernel, tagged with its kind.
+enum MarchKernel : int { kKSearch = 0, kKSplit, kKDeferred, kKHard, kKEmission, kKFused, kKCount };
+struct MarchTimer {
+  cudaEvent_t* ev = nullptr;  // pool of `cap` events
+  int* kind = nullptr;        // kind of the kernel that ends at ev[i]; -1 marks a start
+  int cap = 0, n = 0;
+  // record the next event (false when the pool is full: timing stops there)
+  bool mark(cudaStream_t s, int k) {
+    if (n >= cap) return false;
+    if (cudaEventRecord(ev[n], s) != cudaSuccess) return false;
+    kind[n++] = k;
+    return true;
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -183,7 +201,7 @@ cudaError_t launch_projection(SnapDev snap, const ViewDesc* views, const LineDes
 // the deferred samples' nearest neighbours and their contributions (a second
 // kernel on the same stream).
 cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
-                         cudaStream_t s, int blocks_per_sm_hint, bool imaging);
+                         cudaStream_t s, int blocks_per_sm_hint, bool imaging, MarchTimer* timer = nullptr);
 int march_bins_per_lane(int nlines, int L);
 // Capacity of the deferred-record queue for `items` work items of up to nz samples.
 inline int64_t deferred_capacity(int64_t items, int nz) { return items * ((nz + 63) / 64); }

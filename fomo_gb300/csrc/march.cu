@@ -961,18 +961,23 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
         }
         __syncwarp();
         const int nruns = __popc(fills);
+        if (a.stats && lane == 0 && nruns > 0) {
+          int nwin = 0;
+#pragma unroll
+          for (int l = 0; l < NL; ++l) nwin += lon[l] ? nw[l] : 0;
+          atomicAdd(a.stats + kStatRuns, (unsigned long long)nruns);
+          atomicAdd(a.stats + kStatEx2, 32ull * (unsigned long long)(nruns * nwin));
+        }
         for (int q0 = 0; q0 < nruns; ++q0) {
 #pragma unroll
           for (int l = 0; l < NL; ++l) {
             if (lon[l]) {
               const float4 t = runs[w][q0][l];  // same address in every lane: one broadcast load
-              {
 #pragma unroll
-                for (int m = 0; m < NB; ++m) {
-                  if (m < nw[l]) {
-                    const float q = fmaf(lam[l][m], t.y, t.z);
-                    part[l][m] = fmaf(t.x, ex2_approx(-q * q), part[l][m]);
-                  }
+              for (int m = 0; m < NB; ++m) {
+                if (m < nw[l]) {
+                  const float q = fmaf(lam[l][m], t.y, t.z);
+                  part[l][m] = fmaf(t.x, ex2_approx(-q * q), part[l][m]);
                 }
               }
             }
@@ -1856,22 +1861,35 @@ int march_bins_per_lane(int nlines, int L) {
 // no-allocation path): the fused first pass searches and bins, and the later
 // passes add the deferred samples' emission with atomics.
 cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_stride, int max_windows, int sm_count,
-                         cudaStream_t s, int blocks_per_sm_hint, bool imaging) {
+                         cudaStream_t s, int blocks_per_sm_hint, bool imaging, MarchTimer* timer) {
   if (!a.deferred || a.deferred_cap <= 0 || !a.counter) return cudaErrorInvalidValue;
   const int kind = a.s2 ? kDeferredThomson : (imaging ? kDeferredImaging : kDeferredSpectral);
+  auto mark = [&](int k) {
+    if (timer) timer->mark(s, k);
+  };
+  mark(-1);
   cudaError_t e;
   if (a.npos) {
     e = launch_persistent(march_search, a, ktab, ktab_stride, sm_count, s, blocks_per_sm_hint);
+    mark(kKSearch);
     if (e == cudaSuccess) e = launch_queue(march_split<true>, a, ktab, ktab_stride, sm_count, s, kind);
+    mark(kKSplit);
     if (e == cudaSuccess) e = launch_queue(march_deferred<true>, a, ktab, ktab_stride, sm_count, s, kind);
+    mark(kKDeferred);
     if (e == cudaSuccess && a.hard_cap > 0) e = launch_queue(march_hard<true>, a, ktab, ktab_stride, sm_count, s, kind);
+    mark(kKHard);
     if (e == cudaSuccess) e = launch_emission_pass(a, ktab, ktab_stride, max_windows, sm_count, s, imaging);
+    mark(kKEmission);
     return e;
   }
   e = launch_fused_pass(a, ktab, ktab_stride, max_windows, sm_count, s, blocks_per_sm_hint, imaging);
+  mark(kKFused);
   if (e == cudaSuccess) e = launch_queue(march_split<false>, a, ktab, ktab_stride, sm_count, s, kind);
+  mark(kKSplit);
   if (e == cudaSuccess) e = launch_queue(march_deferred<false>, a, ktab, ktab_stride, sm_count, s, kind);
+  mark(kKDeferred);
   if (e == cudaSuccess && a.hard_cap > 0) e = launch_queue(march_hard<false>, a, ktab, ktab_stride, sm_count, s, kind);
+  mark(kKHard);
   return e;
 }
 

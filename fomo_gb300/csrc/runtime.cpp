@@ -55,6 +55,10 @@ int cuda_err(fomo_ctx* c, cudaError_t e, const char* what) {
 int dev_alloc(fomo_ctx* ctx, void** p, size_t bytes) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;
+  // fault injection for the error paths' tests: the k-th allocation of the
+  // context fails as cudaMalloc would (FOMO_INJECT_ALLOC_FAILURE=k)
+  if (ctx->fail_alloc_at > 0 && ++ctx->alloc_count == ctx->fail_alloc_at)
+    return set_err(ctx, FOMO_ENOMEM, "device allocation failed (injected failure)");
   if (ctx->used + bytes > ctx->budget) {
     std::ostringstream m;
     m << "device allocation of " << bytes << " bytes exceeds the context budget (" << ctx->used << " of "
@@ -887,6 +891,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
   };
   cudaError_t e = cudaMemcpyAsync(db, scr->staging.base, plan.host_bytes, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && scr->staging.copy_done && !capturing) e = cudaEventRecord(scr->staging.copy_done, s);
+  if (ctx->kernel_timing && !capturing) ctx->timer.n = 0;  // the breakdown covers this render
   for (const PlanGroup& G : plan.groups) {
     if (e != cudaSuccess) break;
     SnapRec& snap = ctx->snaps[G.snapshot];
@@ -919,6 +924,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.totpol = G.totpol;
     a.stats = ctx->march_stats;
     if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = record_timing(scr->ev0);
+    MarchTimer* timer = (ctx->kernel_timing && !capturing) ? &ctx->timer : nullptr;
     int rc = FOMO_OK;
     if (G.method == FOMO_METHOD_PROJECTION) {
       for (const auto& z : G.zero_outs)
@@ -942,7 +948,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
           a.total_items = std::min(i1, b + step);
           if (e == cudaSuccess)
             e = launch_march(a, ktab, G.maxnz, G.max_nw, ctx->sm_count, s, G.bps,
-                             G.method == FOMO_METHOD_THOMSON || G.imaging);
+                             G.method == FOMO_METHOD_THOMSON || G.imaging, timer);
         }
         if (e == cudaSuccess && done) rc = (*done)(G, cuts[k], cuts[k + 1]);
       }
@@ -1039,9 +1045,12 @@ int fomo_ctx_create(int device, size_t hbm_budget_bytes, fomo_ctx** out) {
     if (v > 0) ctx->npos_cap = v;
   }
   if (const char* ms = std::getenv("FOMO_MARCH_STATS")) {
-    if (ms[0] == '1' && cudaMalloc(&ctx->march_stats, sizeof(unsigned long long) * kStatCount) == cudaSuccess)
+    if (ms[0] == '1' && cudaMalloc(&ctx->march_stats, sizeof(unsigned long long) * kStatCount) == cudaSuccess) {
       cudaMemset(ctx->march_stats, 0, sizeof(unsigned long long) * kStatCount);
+      ctx->print_stats = true;
+    }
   }
+  if (const char* fa = std::getenv("FOMO_INJECT_ALLOC_FAILURE")) ctx->fail_alloc_at = std::atol(fa);
   const char* tm = std::getenv("FOMO_TIME_MARCH");
   ctx->time_march = !(tm && tm[0] == '0');
   *out = ctx;
@@ -1064,7 +1073,13 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
   dev_free(ctx, ctx->scratch.arena.base);
   dev_free(ctx, ctx->out_arena.base);
   if (ctx->stats_dev) cudaFree(ctx->stats_dev);
-  if (ctx->march_stats) {
+  if (ctx->timer.ev) {
+    for (int i = 0; i < ctx->timer.cap; ++i) cudaEventDestroy(ctx->timer.ev[i]);
+    delete[] ctx->timer.ev;
+    delete[] ctx->timer.kind;
+  }
+  if (ctx->march_stats && !ctx->print_stats) cudaFree(ctx->march_stats);
+  if (ctx->march_stats && ctx->print_stats) {
     unsigned long long h[kStatCount] = {0};
     cudaMemcpy(h, ctx->march_stats, sizeof(h), cudaMemcpyDeviceToHost);
     std::fprintf(stderr,
@@ -1437,6 +1452,67 @@ int fomo_set_march_config(fomo_ctx* ctx, int tile_w, int tile_h, int blocks_per_
   ctx->tile_w = tile_w;
   ctx->tile_h = tile_h;
   ctx->blocks_per_sm = blocks_per_sm;
+  return FOMO_OK;
+}
+
+int fomo_set_profiling(fomo_ctx* ctx, int kernel_timing, int counters) {
+  if (!ctx) return FOMO_EINVAL;
+  cudaSetDevice(ctx->device);
+  static_assert(kKCount == FOMO_KERNEL_COUNT, "kernel kinds of include/fomo_gpu.h");
+  static_assert(kStatCount == FOMO_COUNTER_COUNT, "counters of include/fomo_gpu.h");
+  if (kernel_timing && !ctx->timer.ev) {
+    const int cap = 4096;
+    ctx->timer.ev = new cudaEvent_t[cap]();
+    ctx->timer.kind = new int[cap]();
+    for (int i = 0; i < cap; ++i) {
+      if (cudaEventCreate(&ctx->timer.ev[i]) != cudaSuccess) {
+        for (int k = 0; k < i; ++k) cudaEventDestroy(ctx->timer.ev[k]);
+        delete[] ctx->timer.ev;
+        delete[] ctx->timer.kind;
+        ctx->timer.ev = nullptr;
+        ctx->timer.kind = nullptr;
+        return cuda_err(ctx, cudaGetLastError(), "profiling events");
+      }
+    }
+    ctx->timer.cap = cap;
+  }
+  ctx->kernel_timing = kernel_timing != 0;
+  ctx->timer.n = 0;
+  if (counters && !ctx->march_stats) {
+    FOMO_CUDA(cudaMalloc(&ctx->march_stats, sizeof(unsigned long long) * kStatCount), "profiling counters");
+    FOMO_CUDA(cudaMemset(ctx->march_stats, 0, sizeof(unsigned long long) * kStatCount), "profiling counters");
+  } else if (!counters && ctx->march_stats && !ctx->print_stats) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->march_stats);
+    ctx->march_stats = nullptr;
+  }
+  return FOMO_OK;
+}
+
+int fomo_profile_read(fomo_ctx* ctx, float* kernel_ms, int nk, uint64_t* counters, int nc) {
+  if (!ctx || nk < 0 || nc < 0) return FOMO_EINVAL;
+  cudaSetDevice(ctx->device);
+  if (kernel_ms) {
+    for (int k = 0; k < nk; ++k) kernel_ms[k] = 0.0f;
+    const MarchTimer& t = ctx->timer;
+    if (t.n > 0) FOMO_CUDA(cudaEventSynchronize(t.ev[t.n - 1]), "profiling events");
+    for (int i = 1; i < t.n; ++i) {
+      if (t.kind[i] < 0 || t.kind[i] >= nk) continue;
+      float ms = 0.0f;
+      FOMO_CUDA(cudaEventElapsedTime(&ms, t.ev[i - 1], t.ev[i]), "profiling events");
+      kernel_ms[t.kind[i]] += ms;
+    }
+  }
+  if (counters) {
+    for (int k = 0; k < nc; ++k) counters[k] = 0;
+    if (ctx->march_stats) {
+      unsigned long long h[kStatCount] = {0};
+      FOMO_CUDA(cudaDeviceSynchronize(), "profiling counters");  // the render may be on a caller's stream
+      FOMO_CUDA(cudaMemcpy(h, ctx->march_stats, sizeof(h), cudaMemcpyDeviceToHost), "profiling counters");
+      FOMO_CUDA(cudaMemset(ctx->march_stats, 0, sizeof(h)), "profiling counters");
+      for (int k = 0; k < nc && k < kStatCount; ++k) counters[k] = h[k];
+    }
+  }
   return FOMO_OK;
 }
 

@@ -146,12 +146,17 @@ struct fomo_ctx {
   std::map<std::tuple<int, int, int, double>, float2*> payloads;
   std::map<std::tuple<int, int, int, double>, float> payload_wmax;  // largest FWHM of emitting points
   void* stats_dev = nullptr;  // small device buffer for reductions read back by the host
-  unsigned long long* march_stats = nullptr;  // search counters (FOMO_MARCH_STATS=1), printed at destroy
+  unsigned long long* march_stats = nullptr;  // search counters (profiling; FOMO_MARCH_STATS=1 prints them at destroy)
+  bool print_stats = false;
+  bool kernel_timing = false;  // per-kernel events around the march's kernels (direct launches)
+  fomo::MarchTimer timer;
   fomo::ScratchSet scratch;  // descriptors, per-view tables, Thomson sin^2 chi
   fomo::Arena out_arena;     // device cubes of host-output renders
   std::vector<fomo::ViewReadback> view_readback;
   double cell_occupancy = 2.0;  // target points per grid cell
   int64_t npos_cap = int64_t(1) << 31;  // neighbour-buffer entries per launch (FOMO_NPOS_CAP): 8 GiB
+  long fail_alloc_at = 0;  // FOMO_INJECT_ALLOC_FAILURE: this allocation (1-based) fails, for error-path tests
+  long alloc_count = 0;
   int tile_w = 0, tile_h = 0, blocks_per_sm = 0;
   bool time_march = true;
   float last_ms = 0.0f;

@@ -227,6 +227,59 @@ int fomo_set_march_config(fomo_ctx* ctx, int tile_w, int tile_h, int blocks_per_
 /* Timing of the last render's march kernel (CUDA events on its stream), ms. */
 int fomo_last_march_ms(fomo_ctx* ctx, float* ms);
 
+/* Profiling of later direct renders (not graph replays): CUDA-event times of
+ * each of the march's kernels, and search counters.  kernel_timing / counters:
+ * 1 on, 0 off.  Counting adds atomics to the kernels; timing adds events
+ * between them.  No counterpart in the reference, whose only instrumentation
+ * is a progress bar (fomo-nearestneighbour.cpp:141,228). */
+#define FOMO_KERNEL_SEARCH 0    /* neighbour search (positions to the buffer) */
+#define FOMO_KERNEL_SPLIT 1     /* segments whose candidate list overflowed, searched in parts */
+#define FOMO_KERNEL_DEFERRED 2  /* samples the search left, one lane each */
+#define FOMO_KERNEL_HARD 3      /* deferred samples over a lane's budget, one warp each */
+#define FOMO_KERNEL_EMISSION 4  /* emission pass: binning from the stored neighbours */
+#define FOMO_KERNEL_FUSED 5     /* fused search + emission (the no-allocation path) */
+#define FOMO_KERNEL_COUNT 6
+#define FOMO_COUNTER_SEGMENTS 0      /* 64-sample segments searched */
+#define FOMO_COUNTER_CANDIDATES 1    /* candidates gathered */
+#define FOMO_COUNTER_ROWS 2          /* cell rows visited by the gather */
+#define FOMO_COUNTER_POINTS_LOADED 3 /* points loaded by the gather */
+#define FOMO_COUNTER_NOT_GATHERED 4  /* segments or parts whose capsule overflowed */
+#define FOMO_COUNTER_FALLBACKS 5     /* samples left to the deferred pass */
+#define FOMO_COUNTER_SAMPLES 6       /* LOS samples searched */
+#define FOMO_COUNTER_SCANNED 7       /* candidates scanned by samples */
+#define FOMO_COUNTER_TIES 8          /* samples re-ranked in FP64 */
+#define FOMO_COUNTER_FB_NOCAND 9     /* left: no in-box candidate within the coverage radius */
+#define FOMO_COUNTER_FB_FAR 10       /* left: best candidate beyond the coverage radius */
+#define FOMO_COUNTER_FB_AMBIGUOUS 11 /* left: a candidate within a few ulp of a box face */
+#define FOMO_COUNTER_DEFERRED 12     /* samples searched by the deferred pass */
+#define FOMO_COUNTER_DEFERRED_RECS 13 /* deferred-sample records */
+#define FOMO_COUNTER_HARD 14         /* deferred samples searched by a whole warp */
+#define FOMO_COUNTER_RUNS 15         /* runs of equal neighbours binned by the spectral emission pass */
+#define FOMO_COUNTER_EX2 16          /* ex2 evaluations of the spectral emission pass */
+#define FOMO_COUNTER_COUNT 17
+int fomo_set_profiling(fomo_ctx* ctx, int kernel_timing, int counters);
+/* The last direct render's kernel times (ms) summed per kind (kernel_ms[k] for
+ * FOMO_KERNEL_k, k < nk), and the counters accumulated since they were turned
+ * on (counters[k] for FOMO_COUNTER_k, k < nc; the read zeroes them).  Either
+ * array may be NULL. */
+int fomo_profile_read(fomo_ctx* ctx, float* kernel_ms, int nk, uint64_t* counters, int nc);
+
+/* Ceilings of the march's roofline, measured on the context's device (the
+ * march keeps the snapshot in L2 and is bound by L2 latency, instruction issue
+ * and the SFU, not by HBM): the L2 read bandwidth (a 64 MB buffer streamed
+ * with L2-only loads), the rate of random 16-byte gathers that hit L2 (useful
+ * bytes, the access pattern of the march's candidate and payload loads), and
+ * the SFU's ex2.approx.f32 throughput (one per lambda bin, line and run of
+ * the emission pass).  No counterpart in the reference: a measurement utility
+ * for the benchmark.  Allocates and frees a 64 MB buffer. */
+typedef struct {
+  double l2_read_gbs;
+  double l2_gather_gbs;
+  double ex2_per_s;
+  int sm_count;
+} fomo_ceilings;
+int fomo_measure_ceilings(fomo_ctx* ctx, fomo_ceilings* out);
+
 /* ---- render server: continuous batching of requests as they arrive. */
 typedef struct fomo_server fomo_server;
 typedef struct {

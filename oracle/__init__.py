@@ -23,7 +23,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libfomo_ref.so")
-REF_SRC = "/root/reference/fomo-c/src"
+
+
+def ref_src() -> str:
+    """The reference's fomo-c/src directory as the build recipe (oracle/Makefile)
+    names it; FOMO_REFERENCE_SRC overrides it.  It exists only where the
+    reference tree is mounted (not on the GPU host)."""
+    try:
+        r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True, check=True)
+        return r.stdout.strip()
+    except Exception:
+        return ""
 
 _F = ctypes.POINTER(ctypes.c_float)
 _D = ctypes.POINTER(ctypes.c_double)
@@ -37,7 +47,7 @@ V_COUNT = 12
 def build(ref: bool = True) -> None:
     """Compile liboracle.so (always) and the reference build (when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir(REF_SRC):
+    if ref and os.path.isdir(ref_src()):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8"], check=True)
 
 

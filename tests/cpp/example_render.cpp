@@ -6,12 +6,13 @@
 // abundance file, method, observation type and resolution, render(l, b), read
 // the rendering back and write it.  Arguments:
 //
-//   example_render DATA TABLE METHOD L B NX NY NZ NLAMBDA WIDTH OUT [OPTIONS]
+//   example_render DATA TABLE METHOD L B NX NY NZ NLAMBDA WIDTH OUT [OPTIONS [ABUND]]
 //
 // OUT is the file the rendering is written to with writegoftcube (write
 // options OPTIONS, default 3 = binary + text); the per-view file that render()
 // itself writes (default options: text) goes to OUT's directory as
-// "view-l<deg>b<deg>.txt".  Errors are reported on stderr with exit code 2.
+// "view-l<deg>b<deg>.txt".  ABUND is the abundance file (default "/empty":
+// the tables' own abundances).  Errors are reported on stderr with exit code 2.
 #include <cmath>
 #include <cstdlib>
 #include <fstream>
@@ -42,7 +43,7 @@ int main(int argc, char* argv[]) {
     }
     const std::string method = argv[3];
     if (method.find("Thomson") == std::string::npos) Object.setchiantifile(argv[2]);
-    Object.setabundfile("/empty");
+    Object.setabundfile(argc > 13 ? argv[13] : "/empty");
     Object.setrendermethod(method);
     Object.setobservationtype(FoMo::Spectroscopic);
     const int nx = std::atoi(argv[6]), ny = std::atoi(argv[7]), nz = std::atoi(argv[8]), nl = std::atoi(argv[9]);

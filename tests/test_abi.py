@@ -71,7 +71,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     if not shutil.which("gcc"):
         pytest.skip("no C compiler")
     structs = {"fomo_request": fg.Request, "fomo_view_info": fg.ViewInfo, "fomo_snapshot_info": fg.SnapshotInfo,
-               "fomo_server_config": fg.ServerConfig, "fomo_request_stats": fg.RequestStats}
+               "fomo_server_config": fg.ServerConfig, "fomo_request_stats": fg.RequestStats,
+               "fomo_ceilings": fg.Ceilings}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "fomo_gpu.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')

@@ -73,7 +73,7 @@ def programs(tmp_path_factory):
     out = tmp_path_factory.mktemp("cpp")
     libdir = os.path.dirname(fg.LIB_PATH)
     progs = {}
-    for name in ("example_render", "roundtrip_cube"):
+    for name in ("example_render", "roundtrip_cube", "resolution_units"):
         exe = str(out / name)
         cmd = ["g++", "-std=c++11", "-O1", "-I", os.path.join(ROOT, "include"),
                os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-L", libdir, "-lfomo_gpu",
@@ -147,6 +147,44 @@ def test_example_program_fails_loudly_without_a_gpu(programs, tmp_path):
     assert not os.path.exists(str(tmp_path / "out.txt"))
 
 
+def test_reference_example_program_compiles_unchanged(tmp_path):
+    """The drop-in criterion: the reference's own user program
+    (fomo-c/example/example.cpp), unmodified, compiles against include/FoMo.h
+    and links against libfomo_gpu.so.  Read where the reference tree is
+    mounted (the build recipe names it); skipped elsewhere."""
+    import oracle
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    src = os.path.join(os.path.dirname(oracle.ref_src()), "example", "example.cpp")
+    if not os.path.isfile(src):
+        pytest.skip("the reference tree is not mounted here")
+    if not os.path.exists(fg.LIB_PATH):
+        from fomo_gb300 import build
+        build.build()
+    libdir = os.path.dirname(fg.LIB_PATH)
+    exe = str(tmp_path / "example")
+    r = subprocess.run(["g++", "-std=c++11", "-O1", "-I", os.path.join(ROOT, "include"), src, "-L", libdir,
+                        "-lfomo_gpu", "-Wl,-rpath," + libdir, "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.getsize(exe) > 0
+
+
+def test_angstrom_width_is_converted_with_the_rendering_lambda0(programs, tmp_path):
+    """setresolution with a width below 1 (Angstrom) stores width * c / lambda0
+    of the rendering, whose lambda0 only setchiantifile sets: before it, the
+    default 193.509 A applies (fomo-rendercube.cpp:74-79, fomo-object.cpp:110-116)."""
+    from fomo_gb300 import synth
+    t = synth.line_table(lambda0=171.073)
+    synth.write_table(t, str(tmp_path / "table.dat"))
+    r = subprocess.run([programs["resolution_units"], str(tmp_path / "table.dat")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    w_after, w_before, w_ms = (float(v) for v in r.stdout.split("\n")[-4:-1])  # after the unit warnings
+    assert w_after == 0.6 * fg.SPEED_OF_LIGHT / 171.073
+    assert w_before == 0.6 * fg.SPEED_OF_LIGHT / 193.509
+    assert w_ms == 150000.0
+    assert r.stdout.count("converted to") == 2  # the reference's warning, once per conversion
+
+
 def test_unknown_method_is_an_exception(programs, tmp_path):
     from fomo_gb300 import synth
     data = str(tmp_path / "points.txt")
@@ -204,3 +242,38 @@ def test_example_program_matches_the_reference_files(programs, tmp_path, case):
     view = tmp_path / ("view-l%sb%s.txt" % (deg(l), deg(b)))
     assert view.exists(), sorted(os.listdir(str(tmp_path)))
     assert not (tmp_path / (view.name[:-4] + ".dat")).exists()
+
+
+@pytest.mark.gpu
+def test_example_program_with_an_abundance_file(programs, tmp_path):
+    """FoMoObject::setabundfile on a spectroscopic render: the element's
+    abundance in the file over that in the standard file the tables were made
+    with (FOMO_STANDARD_ABUND) scales the emissivity (fomo-CHIANTI.cpp:264-273).
+    The written cube matches the oracle's render at that ratio; without a
+    standard file the render fails with an error, as the reference's does."""
+    import oracle
+    from fomo_gb300 import synth
+    snap = synth.loop_snapshot(8, seed=2)
+    data = str(tmp_path / "points.txt")
+    _write_data(data, snap)
+    t = synth.line_table(lambda0=193.509, ion="fe_12")
+    synth.write_table(t, str(tmp_path / "table.dat"))
+    rows = {"std.abund": [(1, 12.00, "H"), (26, 7.85, "Fe")], "new.abund": [(1, 12.00, "H"), (26, 8.10, "Fe")]}
+    for name, rr in rows.items():
+        with open(str(tmp_path / name), "w") as f:
+            f.write("".join(f" {z:2d}  {v:6.2f}  {sym}\n" for z, v, sym in rr) + " -1\n")
+    l, b, nx, ny, nz, L, width = 0.35, -0.2, 9, 7, 16, 12, 0.6
+    args = [programs["example_render"], data, "table.dat", "NearestNeighbourGPU", repr(l), repr(b), str(nx), str(ny),
+            str(nz), str(L), repr(width), str(tmp_path / "out.txt"), "1", "new.abund"]
+    env = dict(os.environ, FOMO_STANDARD_ABUND=str(tmp_path / "std.abund"))
+    r = subprocess.run(args, capture_output=True, text=True, cwd=str(tmp_path), env=env)
+    assert r.returncode == 0, r.stderr
+    ours = read_cube(str(tmp_path / "out.dat"))
+    ratio = oracle.abundance_ratio(str(tmp_path / "new.abund"), str(tmp_path / "std.abund"), "fe_12")
+    eps, w = oracle.emission(snap, t, abundratio=ratio)
+    ocube, _, _ = oracle.nn_render(snap, eps, w, t.lambda0, l, b, nx, ny, nz, L, width * fg.SPEED_OF_LIGHT / t.lambda0)
+    assert G.norm_max_err(ours["data"][:, ours["dim"]:].ravel(), ocube.ravel()) <= TOL
+    assert ours["abund"] == "new.abund"
+    env.pop("FOMO_STANDARD_ABUND")
+    r = subprocess.run(args, capture_output=True, text=True, cwd=str(tmp_path), env=env)
+    assert r.returncode == 2 and "abundance" in r.stderr
