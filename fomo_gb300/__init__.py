@@ -16,6 +16,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfomo_gpu.so")
+# the bounds-check build of the same sources (fomo_gb300/build.py): every kernel
+# index checked, an index out of range reported as EDEVICE; for tests
+LIB_CHECKED_PATH = os.path.join(HERE, "libfomo_gpu_checked.so")
 
 OK = 0
 EINVAL, ENOMEM, EADMISSION, EDEVICE, ETIMEOUT, ENOTFOUND, EIO, ETABLE, ECANCELLED, EMETHOD, ENODEVICE = \
@@ -81,6 +84,7 @@ class RequestStats(ctypes.Structure):
 _F = ctypes.POINTER(ctypes.c_float)
 _I32 = ctypes.POINTER(ctypes.c_int32)
 _lib = None
+_lib_checked = None
 
 # (name, argtypes) of every entry point declared in include/fomo_gpu.h
 SIGNATURES = {
@@ -137,18 +141,27 @@ RESTYPES = {"fomo_version": ctypes.c_char_p, "fomo_last_error": ctypes.c_char_p,
             "fomo_server_last_error": ctypes.c_char_p, "fomo_server_context": ctypes.c_void_p}
 
 
-def lib():
-    """Load libfomo_gpu.so (built by fomo_gb300.build); raise if it is missing."""
-    global _lib
+def _load(path: str):
+    if not os.path.exists(path):
+        raise FomoError(ENODEVICE, f"{path} is missing: build it with `python -m fomo_gb300.build`")
+    L = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = RESTYPES.get(name, ctypes.c_int)
+    return L
+
+
+def lib(checked: bool = False):
+    """Load libfomo_gpu.so (built by fomo_gb300.build); raise if it is missing.
+    checked=True loads the bounds-check build instead."""
+    global _lib, _lib_checked
+    if checked:
+        if _lib_checked is None:
+            _lib_checked = _load(LIB_CHECKED_PATH)
+        return _lib_checked
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise FomoError(ENODEVICE, f"{LIB_PATH} is missing: build it with `python -m fomo_gb300.build`")
-        L = ctypes.CDLL(LIB_PATH)
-        for name, args in SIGNATURES.items():
-            fn = getattr(L, name)
-            fn.argtypes = args
-            fn.restype = RESTYPES.get(name, ctypes.c_int)
-        _lib = L
+        _lib = _load(LIB_PATH)
     return _lib
 
 
@@ -163,8 +176,9 @@ def _f32(a):
 class Context:
     """One libfomo_gpu context (device memory, resident snapshots and tables)."""
 
-    def __init__(self, device: int = 0, hbm_budget: int = 0):
-        self._L = lib()
+    def __init__(self, device: int = 0, hbm_budget: int = 0, checked: bool = False):
+        """checked=True: a context of the bounds-check build (libfomo_gpu_checked.so)."""
+        self._L = lib(checked)
         h = ctypes.c_void_p()
         rc = self._L.fomo_ctx_create(device, hbm_budget, ctypes.byref(h))
         if rc != OK:

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "fomo_device.cuh"
 #include "fomo_internal.h"
 
 namespace fomo {
@@ -55,7 +56,9 @@ __global__ void emission_kernel(const float* __restrict__ ne_s, const float* __r
     if (qT >= 0.0f && qT + 1.0f <= (float)(t.nt - 1) && qR >= 0.0f && qR <= (float)(t.nrho - 1)) {
       const int ft = (int)qT, ct = ft + 1, ri = (int)qR;
       const int gi = ri * t.nt + ct;
-      const double x1 = logT[ct], y1 = G[gi], x2 = logT[ft], y2 = G[gi - 1];
+      const int ng = t.nt * t.nrho;
+      const double x1 = logT[FOMO_IDX(ct, t.nt, kSiteTable)], y1 = G[FOMO_IDX(gi, ng, kSiteTable)];
+      const double x2 = logT[FOMO_IDX(ft, t.nt, kSiteTable)], y2 = G[FOMO_IDX(gi - 1, ng, kSiteTable)];
       const double res = __dadd_rn(__ddiv_rn(__dmul_rn(__dsub_rn((double)lT, x1), __dsub_rn(y2, y1)),
                                              __dsub_rn(x2, x1)),
                                    y1);
@@ -144,7 +147,7 @@ __global__ void speed_max_kernel(const float4* __restrict__ vel, int64_t n, unsi
 __global__ void unsort_kernel(const float4* __restrict__ pts, const float2* __restrict__ ew, int64_t n,
                               float* __restrict__ a, float* __restrict__ b) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int o = __float_as_int(pts[i].w);
+    const int64_t o = FOMO_IDX(__float_as_int(pts[i].w), n, kSitePts);
     const float2 v = ew[i];
     a[o] = v.x;
     b[o] = v.y;
@@ -159,6 +162,8 @@ int blocks_for(int64_t n, int threads) {
 }
 
 }  // namespace
+
+FOMO_DEFINE_CHECK_READER(check_word_emission)
 
 cudaError_t launch_emission(const float* ne_s, const float* T_s, int64_t n, TableDev t, float2* ew, cudaStream_t s) {
   const int64_t tab = (int64_t)t.nt * t.nrho + t.nt;

@@ -107,6 +107,7 @@ struct MarchArgs {
   int64_t hard_cap;              // its capacity (0: every deferred sample is searched by one lane)
   int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
   int32_t* npos;                 // neighbour per (work item - item_base, sample), or null (the fused no-allocation march)
+  int64_t npos_cap;              // its entries (index checks of the bounds-check build)
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
   unsigned int* err;             // device error word (bounds-check builds)
@@ -195,6 +196,15 @@ cudaError_t launch_view_finalize(ViewDesc* views, int nviews, double3* ktab, int
 // projection.cu: the projection render of every view of a group (outputs zeroed beforehand)
 cudaError_t launch_projection(SnapDev snap, const ViewDesc* views, const LineDesc* lines, int nviews, int nlines,
                               bool imaging, int sm_count, cudaStream_t s);
+
+// Readers of each file's bounds-check error word (fomo_device.cuh): read and
+// clear on the current device; a non-zero word is the site of the first index
+// out of range.
+cudaError_t check_word_march(unsigned* out);
+cudaError_t check_word_index(unsigned* out);
+cudaError_t check_word_view(unsigned* out);
+cudaError_t check_word_emission(unsigned* out);
+cudaError_t check_word_projection(unsigned* out);
 
 // march.cu
 // The march: the first search pass and the emission sums of every ray, then

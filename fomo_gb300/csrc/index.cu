@@ -61,7 +61,7 @@ __global__ void bin_kernel(const float* __restrict__ x, const float* __restrict_
     int cz = cell_coord(z[i], g.oz, g.inv_h, g.dz);
     int c = (cz * g.dy + cy) * g.dx + cx;
     cell_of[i] = c;
-    atomicAdd(&counts[c], 1);
+    atomicAdd(&counts[FOMO_IDX(c, (int64_t)g.dx * g.dy * g.dz, kSiteIndexBuild)], 1);
   }
 }
 
@@ -155,8 +155,10 @@ __global__ void scatter_kernel(const float* __restrict__ x, const float* __restr
                                const int* __restrict__ cell_start, int* __restrict__ fill, float4* __restrict__ pts,
                                float4* __restrict__ vel, float* __restrict__ ne_s, float* __restrict__ T_s) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    // cell_of < cells by construction (bin_kernel clamps every coordinate); its
+    // capacity is the number of points, which also bounds every position
     int c = cell_of[i];
-    int pos = cell_start[c] + atomicAdd(&fill[c], 1);
+    int pos = FOMO_IDX(cell_start[c] + atomicAdd(&fill[c], 1), n, kSiteIndexBuild);
     pts[pos] = make_float4(x[i], y[i], z[i], __int_as_float((int)i));
     vel[pos] = make_float4(vx[i], vy[i], vz[i], 0.0f);
     ne_s[pos] = ne[i];
@@ -169,6 +171,9 @@ __global__ void sort_cells_kernel(const int* __restrict__ cell_start, int64_t nc
                                   float4* __restrict__ vel, float* __restrict__ ne_s, float* __restrict__ T_s) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
     int b = cell_start[c], e = cell_start[c + 1];
+    // the cell's points lie in [0, cell_start[ncells]); a range outside it is
+    // recorded and skipped in the bounds-check build
+    if (e > b && FOMO_IDX(e - 1, cell_start[ncells], kSiteIndexBuild) != e - 1) continue;
     for (int i = b + 1; i < e; ++i) {
       float4 p = pts[i];
       float4 v = vel[i];
@@ -198,6 +203,8 @@ int grid_blocks(int64_t n, int threads) {
 }
 
 }  // namespace
+
+FOMO_DEFINE_CHECK_READER(check_word_index)
 
 cudaError_t launch_aabb(const float* x, const float* y, const float* z, int64_t n, unsigned int* bits6,
                         cudaStream_t s) {

@@ -103,6 +103,9 @@ struct BoxQ {
   float tx, ty, tz, lox, loy, loz, hix, hiy, hiz;
 };
 
+// Entries of the grid's cell_start array (its cells + 1).
+__device__ __forceinline__ int64_t cell_entries(const GridParams& g) { return (int64_t)g.dx * g.dy * g.dz + 1; }
+
 __device__ __forceinline__ float axis_gap(int c, float t, float o, float h) {
   const float lo = fmaf((float)c - kCellMargin, h, o);
   const float hi = fmaf((float)c + 1.0f + kCellMargin, h, o);
@@ -115,6 +118,30 @@ __device__ __forceinline__ double exact_dist2(float px, float py, float pz, floa
   const double dz = __dsub_rn((double)pz, (double)tz);
   return __dadd_rn(__dmul_rn(dz, dz), __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dx, dx)));
 }
+
+// Row rr of a box of rows nyr wide: (rr / nyr, rr % nyr) for 0 <= rr < 2^20 and
+// 1 <= nyr < 2^20.  The FP32 estimate of the quotient (inv = the FP32
+// reciprocal of nyr) is off by at most one here, and one correction step makes
+// it exact (an integer division by a variable costs several times as many
+// instructions).
+__device__ __forceinline__ int row_div(int rr, int nyr, float inv, int& rem) {
+  int q = __float2int_rz((float)rr * inv);
+  int r = rr - q * nyr;
+  if (r < 0) {
+    --q;
+    r += nyr;
+  } else if (r >= nyr) {
+    ++q;
+    r -= nyr;
+  }
+  rem = r;
+  return q;
+}
+
+// The local point spacing, in cells, at a mean cell occupancy of mocc points:
+// mocc^(-1/3), from the SFU's log2 and exp2 (a heuristic for the gather radius;
+// a few ulp do not matter).
+__device__ __forceinline__ float spacing_cells(float mocc) { return ex2_approx(__log2f(mocc) * (-1.0f / 3.0f)); }
 
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
@@ -152,6 +179,7 @@ struct RayCtx {
   unsigned int item;  // work item of the ray (recorded with its deferred samples)
   double A0, A1, A2, md;
   float mdf;
+  int nz;             // LOS samples of the ray's view (the length of its LOS table)
   const double3* kt;
 };
 
@@ -181,8 +209,8 @@ __device__ __forceinline__ bool ray_of_item(const MarchArgs& a, const double3* k
   if (i >= ny || j >= nx) return false;
   // ray position in the image plane (nn:152-153, tabulated per view by the
   // finalize kernel) and the per-ray terms of the derotation (nn:165)
-  const double x = V->xt[j];
-  const double y = V->yt[i];
+  const double x = V->xt[FOMO_IDX(j, nx, kSiteRayXY)];
+  const double y = V->yt[FOMO_IDX(i, ny, kSiteRayXY)];
   const double cb = V->cb, sb = V->sb, cl = V->cl, sl = V->sl;
   r.v = v;
   r.i = i;
@@ -194,6 +222,7 @@ __device__ __forceinline__ bool ray_of_item(const MarchArgs& a, const double3* k
   r.md = V->md;
   r.mdf = __double2float_rn(V->md);
   r.kt = ktab + (int64_t)v * ktab_stride;
+  r.nz = V->nz;
   return true;
 }
 
@@ -213,7 +242,7 @@ __device__ __forceinline__ bool next_ray(const MarchArgs& a, const double3* ktab
 
 // LOS sample k: derotated position (nn:162-165) in FP64.
 __device__ __forceinline__ void sample_pos(const RayCtx& r, int k, double& p0, double& p1, double& p2) {
-  const double3 zt = r.kt[k];
+  const double3 zt = r.kt[FOMO_IDX(k, r.nz, kSiteKtab)];
   p0 = __dadd_rn(r.A0, zt.x);
   p1 = __dsub_rn(r.A1, zt.y);
   p2 = __dadd_rn(r.A2, zt.z);
@@ -323,11 +352,12 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
       if (px >= g.minx && px <= g.maxx && py >= g.miny && py <= g.maxy && pz >= g.minz && pz <= g.maxz) {
         const int c = (cell_coord(pz, g.oz, g.inv_h, g.dz) * g.dy + cell_coord(py, g.oy, g.inv_h, g.dy)) * g.dx +
                       cell_coord(px, g.ox, g.inv_h, g.dx);
-        occ = __ldg(S.cell_start + c + 1) - __ldg(S.cell_start + c);
+        occ = __ldg(S.cell_start + FOMO_IDX(c + 1, cell_entries(g), kSiteCellStart)) -
+              __ldg(S.cell_start + FOMO_IDX(c, cell_entries(g), kSiteCellStart));
       }
     }
     const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
-    const float aloc = g.h * cbrtf(1.0f / mocc);
+    const float aloc = g.h * spacing_cells(mocc);
     const float R = fminf(r.mdf * 1.7321f * 1.0001f, kRScale * aloc);
     const float amax =
         fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
@@ -354,11 +384,14 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
         const float inv_dy = fabsf(sdy) > 1e-30f ? 1.0f / sdy : 0.0f;
         const float inv_dz = fabsf(sdz) > 1e-30f ? 1.0f / sdz : 0.0f;
         const unsigned lt = (1u << lane) - 1u;
+        const float inv_nyr = 1.0f / (float)nyr;
         for (int rb = 0; rb < nrows && count <= kSegCap; rb += 32) {
           const int rr = rb + lane;
           int n = 0, base = 0;
           if (rr < nrows) {
-            const int jy = y0 + rr % nyr, kz = z0 + rr / nyr;
+            int ry;
+            const int rz = row_div(rr, nyr, inv_nyr, ry);
+            const int jy = y0 + ry, kz = z0 + rz;
             float slo = 0.0f, shi = 1.0f;
             clip_interval(ay, sdy, inv_dy, fmaf((float)jy, g.h, g.oy) - m - Rg,
                           fmaf((float)(jy + 1), g.h, g.oy) + m + Rg, slo, shi);
@@ -372,8 +405,8 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
               const int c1 = min(x1, cell_coord(fmaxf(xa, xb) + xm, g.ox, g.inv_h, g.dx));
               if (c0 <= c1) {
                 const int rowbase = (kz * g.dy + jy) * g.dx;
-                base = __ldg(S.cell_start + rowbase + c0);
-                n = __ldg(S.cell_start + rowbase + c1 + 1) - base;
+                base = __ldg(S.cell_start + FOMO_IDX(rowbase + c0, cell_entries(g), kSiteCellStart));
+                n = __ldg(S.cell_start + FOMO_IDX(rowbase + c1 + 1, cell_entries(g), kSiteCellStart)) - base;
               }
             }
           }
@@ -392,7 +425,7 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
             int p = 0, bk = 0;
             if (i < total) {
               p = ob + (i - oe);
-              q = __ldg(S.pts + p);
+              q = __ldg(S.pts + FOMO_IDX(p, S.n, kSitePts));
               const float wx = q.x - ax, wy = q.y - ay, wz = q.z - az;
               float s = fmaf(wz, sdz, fmaf(wy, sdy, wx * sdx)) * inv_len2;
               s = fminf(fmaxf(s, 0.0f), 1.0f);
@@ -427,7 +460,7 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
     sm.cursor[lane] = 0;
     sm.cursor[lane + 32] = 0;
     __syncwarp();
-    for (int c = lane; c < ncand; c += 32) atomicAdd(&sm.cursor[sm.cb[c]], 1);
+    for (int c = lane; c < ncand; c += 32) atomicAdd(&sm.cursor[FOMO_IDX(sm.cb[c], kSeg, kSiteSmem)], 1);
     __syncwarp();
     {
       const int h0 = sm.cursor[2 * lane], h1 = sm.cursor[2 * lane + 1];
@@ -442,7 +475,7 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
     }
     __syncwarp();
     for (int c = lane; c < ncand; c += 32) {
-      const int dst = kSegCap + atomicAdd(&sm.cursor[sm.cb[c]], 1);
+      const int dst = kSegCap + FOMO_IDX(atomicAdd(&sm.cursor[FOMO_IDX(sm.cb[c], kSeg, kSiteSmem)], 1), kSegCap, kSiteSmem);
       sm.q[dst] = sm.q[c];
       sm.pos[dst] = sm.pos[c];
     }
@@ -511,8 +544,8 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
             ++st_ties;
             bi = exact_rerank_list(sq, c0, c1, t_x, t_y, t_z, md_in, b1 * (1.0f + kRelTie));
           }
-          pres = spos[bi];
-          ores = __float_as_int(sq[bi].w);
+          pres = spos[FOMO_IDX(bi, kSegCap, kSiteSmem)];
+          ores = __float_as_int(sq[FOMO_IDX(bi, kSegCap, kSiteSmem)].w);
         }
         if (stats && !accept)  // rare: counted where it happens
           atomicAdd(stats + (amb ? kStatFbAmb : (bi < 0 ? kStatFbNoCand : kStatFbFar)), 1ull);
@@ -597,11 +630,12 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
     if (px >= g.minx && px <= g.maxx && py >= g.miny && py <= g.maxy && pz >= g.minz && pz <= g.maxz) {
       const int c = (cell_coord(pz, g.oz, g.inv_h, g.dz) * g.dy + cell_coord(py, g.oy, g.inv_h, g.dy)) * g.dx +
                     cell_coord(px, g.ox, g.inv_h, g.dx);
-      occ = __ldg(S.cell_start + c + 1) - __ldg(S.cell_start + c);
+      occ = __ldg(S.cell_start + FOMO_IDX(c + 1, cell_entries(g), kSiteCellStart)) -
+            __ldg(S.cell_start + FOMO_IDX(c, cell_entries(g), kSiteCellStart));
     }
   }
   const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
-  const float aloc = g.h * cbrtf(1.0f / mocc);
+  const float aloc = g.h * spacing_cells(mocc);
   const float R = fminf(r.mdf * 1.7321f * 1.0001f, kRScale * aloc);
   const float amax =
       fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
@@ -628,11 +662,14 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
       const float inv_dy = fabsf(sdy) > 1e-30f ? 1.0f / sdy : 0.0f;
       const float inv_dz = fabsf(sdz) > 1e-30f ? 1.0f / sdz : 0.0f;
       const unsigned lt = (1u << lane) - 1u;
+      const float inv_nyr = 1.0f / (float)nyr;
       for (int rb = 0; rb < nrows && count <= kSegCap; rb += 32) {
         const int rr = rb + lane;
         int n = 0, base = 0;
         if (rr < nrows) {
-          const int jy = y0 + rr % nyr, kz = z0 + rr / nyr;
+          int ry;
+          const int rz = row_div(rr, nyr, inv_nyr, ry);
+          const int jy = y0 + ry, kz = z0 + rz;
           float slo = 0.0f, shi = 1.0f;
           clip_interval(ay, sdy, inv_dy, fmaf((float)jy, g.h, g.oy) - m - Rg, fmaf((float)(jy + 1), g.h, g.oy) + m + Rg,
                         slo, shi);
@@ -646,8 +683,8 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
             const int c1 = min(x1, cell_coord(fmaxf(xa, xb) + xm, g.ox, g.inv_h, g.dx));
             if (c0 <= c1) {
               const int rowbase = (kz * g.dy + jy) * g.dx;
-              base = __ldg(S.cell_start + rowbase + c0);
-              n = __ldg(S.cell_start + rowbase + c1 + 1) - base;
+              base = __ldg(S.cell_start + FOMO_IDX(rowbase + c0, cell_entries(g), kSiteCellStart));
+              n = __ldg(S.cell_start + FOMO_IDX(rowbase + c1 + 1, cell_entries(g), kSiteCellStart)) - base;
             }
           }
         }
@@ -666,7 +703,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
           int p = 0, bk = 0;
           if (i < total) {
             p = ob + (i - oe);
-            q = __ldg(S.pts + p);
+            q = __ldg(S.pts + FOMO_IDX(p, S.n, kSitePts));
             const float wx = q.x - ax, wy = q.y - ay, wz = q.z - az;
             float s = fmaf(wz, sdz, fmaf(wy, sdy, wx * sdx)) * inv_len2;
             s = fminf(fmaxf(s, 0.0f), 1.0f);
@@ -694,7 +731,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
   sm.cursor[lane] = 0;
   sm.cursor[lane + 32] = 0;
   __syncwarp();
-  for (int c = lane; c < ncand; c += 32) atomicAdd(&sm.cursor[sm.cb[c]], 1);
+  for (int c = lane; c < ncand; c += 32) atomicAdd(&sm.cursor[FOMO_IDX(sm.cb[c], kSeg, kSiteSmem)], 1);
   __syncwarp();
   {
     const int h0 = sm.cursor[2 * lane], h1 = sm.cursor[2 * lane + 1];
@@ -709,7 +746,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
   }
   __syncwarp();
   for (int c = lane; c < ncand; c += 32) {
-    const int dst = kSegCap + atomicAdd(&sm.cursor[sm.cb[c]], 1);
+    const int dst = kSegCap + FOMO_IDX(atomicAdd(&sm.cursor[FOMO_IDX(sm.cb[c], kSeg, kSiteSmem)], 1), kSegCap, kSiteSmem);
     sm.q[dst] = sm.q[c];
     sm.pos[dst] = sm.pos[c];
   }
@@ -780,8 +817,8 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
           ++st_ties;
           bi = exact_rerank_list(sq, c0, c1, t_x, t_y, t_z, md_in, b1 * (1.0f + kRelTie));
         }
-        pres = spos[bi];
-        ores = __float_as_int(sq[bi].w);
+        pres = spos[FOMO_IDX(bi, kSegCap, kSiteSmem)];
+        ores = __float_as_int(sq[FOMO_IDX(bi, kSegCap, kSiteSmem)].w);
       }
       if (stats && !accept)  // rare: counted where it happens
         atomicAdd(stats + (amb ? kStatFbAmb : (bi < 0 ? kStatFbNoCand : kStatFbFar)), 1ull);
@@ -809,7 +846,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
     const unsigned long long k = atomicAdd(a.counter + (over ? kCtrOverflow : kCtrDeferred), 1ull);
     const int64_t slot = over ? a.deferred_cap - 1 - (int64_t)k : (int64_t)k;
     if (slot >= 0 && slot < a.deferred_cap)  // always: the capacity is one record per segment
-      a.deferred[slot] = make_uint4(r.item, (unsigned)s0, f0, f1);
+      a.deferred[FOMO_IDX(slot, a.deferred_cap, kSiteDeferred)] = make_uint4(r.item, (unsigned)s0, f0, f1);
   }
   if (stats) {
     const unsigned sc = __reduce_add_sync(kFull, (unsigned)st_scanned);
@@ -861,8 +898,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSearch) march_search(MarchAr
       for (int h = 0; h < 2; ++h) {
         const int k = s0 + 32 * h + lane;
         if (k < nz) {
-          __stcs(npos + k, h ? posv[1] : posv[0]);
-          if (nnout) nnout[ray * nz + k] = h ? origv[1] : origv[0];
+          __stcs(a.npos + FOMO_IDX(npos - a.npos + k, a.npos_cap, kSiteNpos), h ? posv[1] : posv[0]);
+          if (nnout) nnout[FOMO_IDX(ray * nz + k, (int64_t)V->nx * V->ny * nz, kSiteNnIdx)] = h ? origv[1] : origv[0];
         }
       }
     }
@@ -909,7 +946,7 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
         comp[l][m] = 0.0f;
         part[l][m] = 0.0f;
         // lambdaval (nn:200), evaluated in FP64 on the host, stored FP32
-        lam[l][m] = (m < nw[l] && il < L) ? __ldg(LD[l].lam + il) : 3.0e30f;
+        lam[l][m] = (m < nw[l] && il < L) ? __ldg(LD[l].lam + FOMO_IDX(il, L, kSiteLam)) : 3.0e30f;
       }
     }
     int32_t* nnout = (!SHADE && a.nn_idx) ? a.nn_idx[r.v] : nullptr;
@@ -918,8 +955,9 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
     for (int s0 = 0; s0 < nz; s0 += kSeg) {
       int posv[2], origv[2];
       if (SHADE) {
-        posv[0] = s0 + lane < nz ? __ldcs(npos + s0 + lane) : -1;
-        posv[1] = s0 + 32 + lane < nz ? __ldcs(npos + s0 + 32 + lane) : -1;
+        posv[0] = s0 + lane < nz ? __ldcs(a.npos + FOMO_IDX(npos - a.npos + s0 + lane, a.npos_cap, kSiteNpos)) : -1;
+        posv[1] = s0 + 32 + lane < nz ? __ldcs(a.npos + FOMO_IDX(npos - a.npos + s0 + 32 + lane, a.npos_cap, kSiteNpos))
+                                      : -1;
       } else {
         segment_search(a, r, s0, nz, sm, posv, origv);
       }
@@ -928,7 +966,8 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
         const int k = s0 + 32 * h + lane;
         const bool active = k < nz;
         const int pos = h ? posv[1] : posv[0];
-        if (nnout && active) nnout[ray * nz + k] = h ? origv[1] : origv[0];
+        if (nnout && active)
+          nnout[FOMO_IDX(ray * nz + k, (int64_t)V->nx * V->ny * nz, kSiteNnIdx)] = h ? origv[1] : origv[0];
         // runs of equal neighbours
         const int prev = __shfl_up_sync(kFull, pos, 1);
         const bool start = active && (lane == 0 || pos != prev);
@@ -946,13 +985,13 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
           const unsigned later = starts & ~((2u << lane) - 1u);
           const int e = later ? (__ffs(later) - 1) : endlane;
           const float cnt = (float)(e - lane);
-          const float4 vv = __ldg(a.snap.vel + pos);
+          const float4 vv = __ldg(a.snap.vel + FOMO_IDX(pos, a.snap.n, kSitePts));
           const float vlos = fmaf(uz, vv.z, fmaf(uy, vv.y, ux * vv.x));
           float4* dst = runs[w][__popc(fills & ((1u << lane) - 1u))];
 #pragma unroll
           for (int l = 0; l < NL; ++l) {
             if (lon[l]) {
-              const float2 pw = __ldg(ew[l] + pos);
+              const float2 pw = __ldg(ew[l] + FOMO_IDX(pos, a.snap.n, kSitePts));
               const float sc = __fdividef(2.0f, pw.y);  // exp(-4 ln2 (d/w)^2) = 2^(-(2d/w)^2)
               dst[l] = pw.x != 0.0f ? make_float4(pw.x * cnt, sc, -(vlos * shk[l]) * sc, 0.0f)
                                     : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -997,14 +1036,16 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtas)
     for (int l = 0; l < NL; ++l) {
       if (lon[l]) {
         const double scale = LD[l].is_dn ? V->scale_dn : V->scale;
-        float* out = LD[l].out + ray * L;
+        float* out = LD[l].out;
+        const int64_t ncube = (int64_t)nx * V->ny * L;
         const int wlo = ws[l], whi = ws[l] + 32 * nw[l];
         for (int il = lane; il < L; il += 32)
-          if (il < wlo || il >= whi) out[il] = 0.0f;  // below 2^-64 of every peak
+          if (il < wlo || il >= whi) out[FOMO_IDX(ray * L + il, ncube, kSiteCube)] = 0.0f;  // below 2^-64 of every peak
 #pragma unroll
         for (int m = 0; m < NB; ++m) {
           const int il = wlo + m * 32 + lane;
-          if (m < nw[l] && il < L) out[il] = __double2float_rn(__dmul_rn(scale, (double)acc[l][m]));
+          if (m < nw[l] && il < L)
+            out[FOMO_IDX(ray * L + il, ncube, kSiteCube)] = __double2float_rn(__dmul_rn(scale, (double)acc[l][m]));
         }
       }
     }
@@ -1045,8 +1086,9 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtasImag
     for (int s0 = 0; s0 < nz; s0 += kSeg) {
       int posv[2], origv[2];
       if (SHADE) {
-        posv[0] = s0 + lane < nz ? __ldcs(npos + s0 + lane) : -1;
-        posv[1] = s0 + 32 + lane < nz ? __ldcs(npos + s0 + 32 + lane) : -1;
+        posv[0] = s0 + lane < nz ? __ldcs(a.npos + FOMO_IDX(npos - a.npos + s0 + lane, a.npos_cap, kSiteNpos)) : -1;
+        posv[1] = s0 + 32 + lane < nz ? __ldcs(a.npos + FOMO_IDX(npos - a.npos + s0 + 32 + lane, a.npos_cap, kSiteNpos))
+                                      : -1;
       } else {
         segment_search(a, r, s0, nz, sm, posv, origv);
       }
@@ -1055,7 +1097,8 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtasImag
         const int k = s0 + 32 * h + lane;
         const bool active = k < nz;
         const int pos = h ? posv[1] : posv[0];
-        if (nnout && active) nnout[ray * nz + k] = h ? origv[1] : origv[0];
+        if (nnout && active)
+          nnout[FOMO_IDX(ray * nz + k, (int64_t)V->nx * V->ny * nz, kSiteNnIdx)] = h ? origv[1] : origv[0];
 #pragma unroll
         for (int l = 0; l < NL; ++l) {
           if (lon[l]) {
@@ -1063,9 +1106,11 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtasImag
             if (pos >= 0) {
               if (THOMSON) {
                 // pB = pol * sin^2 chi, clamped at 0 (thomson:325-338)
-                val = fmaxf(__ldg(a.totpol + pos).y * __ldg(s2v + pos), 0.0f);
+                val = fmaxf(__ldg(a.totpol + FOMO_IDX(pos, a.snap.n, kSitePts)).y *
+                                __ldg(s2v + FOMO_IDX(pos, a.snap.n, kSiteS2)),
+                            0.0f);
               } else {
-                val = __ldg(LD[l].ew + pos).x;  // imaging adds the peak (nn:217-225)
+                val = __ldg(LD[l].ew + FOMO_IDX(pos, a.snap.n, kSitePts)).x;  // imaging adds the peak (nn:217-225)
               }
             }
             const float cs = warp_sum(val);
@@ -1078,7 +1123,8 @@ __global__ void __launch_bounds__(kThreads, SHADE ? kMinCtasShade : kMinCtasImag
 #pragma unroll
       for (int l = 0; l < NL; ++l)
         if (lon[l])
-          LD[l].out[ray] = __double2float_rn(__dmul_rn(LD[l].is_dn ? V->scale_dn : V->scale, (double)acc[l]));
+          LD[l].out[FOMO_IDX(ray, (int64_t)nx * V->ny, kSiteCube)] =
+              __double2float_rn(__dmul_rn(LD[l].is_dn ? V->scale_dn : V->scale, (double)acc[l]));
     }
   }
 }
@@ -1137,7 +1183,8 @@ __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p
     budget -= (p1 - p0 > kLaneDense) ? 0x3fffffff : 1 + (p1 - p0);
     if (budget < 0) return;
   }
-  for (int p = p0; p < p1; ++p) scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
+  for (int p = p0; p < p1; ++p)
+    scan_point<EXACT>(__ldg(S.pts + FOMO_IDX(p, S.n, kSitePts)), p, q, band, best, second, bpos, borig, bD);
 }
 
 // One lane's walk over the rings of cells around the target's cell c (clamped
@@ -1195,16 +1242,19 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
             x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
           }
           if (x0 <= x1)
-            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + rowbase + x0), __ldg(S.cell_start + rowbase + x1 + 1), band,
-                             best, second, bpos, borig, bD, budget);
+            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + FOMO_IDX(rowbase + x0, cell_entries(g), kSiteCellStart)),
+                                     __ldg(S.cell_start + FOMO_IDX(rowbase + x1 + 1, cell_entries(g), kSiteCellStart)),
+                                     band, best, second, bpos, borig, bD, budget);
         } else {
           // a row inside the ring's y-z square: only its two end cells are on the ring
           if (has_l && fmaf(gxl, gxl, gyz) <= bound)
-            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + rowbase + xl), __ldg(S.cell_start + rowbase + xl + 1), band,
-                             best, second, bpos, borig, bD, budget);
+            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + FOMO_IDX(rowbase + xl, cell_entries(g), kSiteCellStart)),
+                                     __ldg(S.cell_start + FOMO_IDX(rowbase + xl + 1, cell_entries(g), kSiteCellStart)),
+                                     band, best, second, bpos, borig, bD, budget);
           if (has_r && fmaf(gxr, gxr, gyz) <= (EXACT ? bound : best * (1.0f + kRelPrune)))
-            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + rowbase + xr), __ldg(S.cell_start + rowbase + xr + 1), band,
-                             best, second, bpos, borig, bD, budget);
+            lane_scan<EXACT, BUDGET>(S, q, __ldg(S.cell_start + FOMO_IDX(rowbase + xr, cell_entries(g), kSiteCellStart)),
+                                     __ldg(S.cell_start + FOMO_IDX(rowbase + xr + 1, cell_entries(g), kSiteCellStart)),
+                                     band, best, second, bpos, borig, bD, budget);
         }
       }
     }
@@ -1335,17 +1385,17 @@ __device__ __forceinline__ void warp_rings(const SnapDev& S, const BoxQ& q, cons
               x1 = min(x1, cell_coord(q.tx + rx, g.ox, g.inv_h, g.dx));
             }
             if (x0 <= x1) {
-              a0 = __ldg(S.cell_start + rowbase + x0);
-              n0 = __ldg(S.cell_start + rowbase + x1 + 1) - a0;
+              a0 = __ldg(S.cell_start + FOMO_IDX(rowbase + x0, cell_entries(g), kSiteCellStart));
+              n0 = __ldg(S.cell_start + FOMO_IDX(rowbase + x1 + 1, cell_entries(g), kSiteCellStart)) - a0;
             }
           } else {
             if (has_l && fmaf(gxl, gxl, gyz) <= bound) {
-              a0 = __ldg(S.cell_start + rowbase + xl);
-              n0 = __ldg(S.cell_start + rowbase + xl + 1) - a0;
+              a0 = __ldg(S.cell_start + FOMO_IDX(rowbase + xl, cell_entries(g), kSiteCellStart));
+              n0 = __ldg(S.cell_start + FOMO_IDX(rowbase + xl + 1, cell_entries(g), kSiteCellStart)) - a0;
             }
             if (has_r && fmaf(gxr, gxr, gyz) <= bound) {
-              a1 = __ldg(S.cell_start + rowbase + xr);
-              n1 = __ldg(S.cell_start + rowbase + xr + 1) - a1;
+              a1 = __ldg(S.cell_start + FOMO_IDX(rowbase + xr, cell_entries(g), kSiteCellStart));
+              n1 = __ldg(S.cell_start + FOMO_IDX(rowbase + xr + 1, cell_entries(g), kSiteCellStart)) - a1;
             }
           }
         }
@@ -1362,7 +1412,7 @@ __device__ __forceinline__ void warp_rings(const SnapDev& S, const BoxQ& q, cons
         if (i < total) {
           const int k = i - oe;
           const int p = k < on0 ? oa0 + k : oa1 + (k - on0);
-          scan_point<EXACT>(__ldg(S.pts + p), p, q, band, best, second, bpos, borig, bD);
+          scan_point<EXACT>(__ldg(S.pts + FOMO_IDX(p, S.n, kSitePts)), p, q, band, best, second, bpos, borig, bD);
         }
       }
     }
@@ -1424,6 +1474,7 @@ __device__ __forceinline__ RayCtx shfl_ray(const RayCtx& r, int src) {
   o.A2 = __shfl_sync(kFull, r.A2, src);
   o.md = __shfl_sync(kFull, r.md, src);
   o.mdf = __shfl_sync(kFull, r.mdf, src);
+  o.nz = __shfl_sync(kFull, r.nz, src);
   o.kt = reinterpret_cast<const double3*>(
       __shfl_sync(kFull, (unsigned long long)reinterpret_cast<uintptr_t>(r.kt), src));
   return o;
@@ -1454,19 +1505,21 @@ __device__ __forceinline__ void add_emission(const MarchArgs& a, const RayCtx& r
       const double scale = D.is_dn ? V->scale_dn : V->scale;
       for (int m = 0; m < D.nw; ++m) {
         const int il = D.wstart + 32 * m + lane;
-        const float lamv = il < L ? __ldg(D.lam + il) : 3.0e30f;
+        const float lamv = il < L ? __ldg(D.lam + FOMO_IDX(il, L, kSiteLam)) : 3.0e30f;
         float part = 0.0f;
         for (int f = 0; f < n; ++f) {
           const int p = sp[f];
           if (p < 0) continue;
-          const float2 pw = __ldg(D.ew + p);
+          const float2 pw = __ldg(D.ew + FOMO_IDX(p, a.snap.n, kSitePts));
           if (pw.x == 0.0f) continue;  // intpolpeak ? ... : 0 (nn:204)
           const float sc = __fdividef(2.0f, pw.y);
           const float ns = -(sv[f] * D.shift_k) * sc;
           const float q = fmaf(lamv, sc, ns);
           part = fmaf(pw.x, ex2_approx(-q * q), part);
         }
-        if (il < L && part != 0.0f) atomicAdd(D.out + ray * L + il, __double2float_rn(__dmul_rn(scale, (double)part)));
+        if (il < L && part != 0.0f)
+          atomicAdd(D.out + FOMO_IDX(ray * L + il, (int64_t)V->nx * V->ny * L, kSiteCube),
+                    __double2float_rn(__dmul_rn(scale, (double)part)));
       }
     }
   } else {
@@ -1477,11 +1530,15 @@ __device__ __forceinline__ void add_emission(const MarchArgs& a, const RayCtx& r
       float val = 0.0f;
       for (int f = lane; f < n; f += 32) {
         const int p = sp[f];
-        if (p >= 0) val += s2v ? fmaxf(__ldg(a.totpol + p).y * __ldg(s2v + p), 0.0f) : __ldg(D.ew + p).x;
+        if (p >= 0) {
+          const int64_t pc = FOMO_IDX(p, a.snap.n, kSitePts);
+          val += s2v ? fmaxf(__ldg(a.totpol + pc).y * __ldg(s2v + pc), 0.0f) : __ldg(D.ew + pc).x;
+        }
       }
       const float sum = warp_sum(val);
       if (lane == 0 && sum != 0.0f)
-        atomicAdd(D.out + ray, __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
+        atomicAdd(D.out + FOMO_IDX(ray, (int64_t)V->nx * V->ny, kSiteCube),
+                  __double2float_rn(__dmul_rn(D.is_dn ? V->scale_dn : V->scale, (double)sum)));
     }
   }
 }
@@ -1491,13 +1548,14 @@ __device__ __forceinline__ void add_emission(const MarchArgs& a, const RayCtx& r
 // the slowest searches: started early, they do not make the kernel's tail),
 // then the first pass's records from the front.
 __device__ __forceinline__ DeferredRec deferred_at(const MarchArgs& a, int64_t nback, int64_t ri) {
-  return ri < nback ? a.deferred[a.deferred_cap - 1 - ri] : a.deferred[ri - nback];
+  return ri < nback ? a.deferred[FOMO_IDX(a.deferred_cap - 1 - ri, a.deferred_cap, kSiteDeferred)]
+                    : a.deferred[FOMO_IDX(ri - nback, a.deferred_cap, kSiteDeferred)];
 }
 
 // Sample k of work item `item` in the position buffer (rows of `stride`
 // entries from the launch's first work item).
 __device__ __forceinline__ int32_t* npos_at(const MarchArgs& a, unsigned item, int k, int stride) {
-  return a.npos + ((int64_t)item - a.item_base) * stride + k;
+  return a.npos + FOMO_IDX(((int64_t)item - a.item_base) * stride + k, a.npos_cap, kSiteNpos);
 }
 
 // A deferred sample's result: its NN index, and its neighbour -- into the
@@ -1509,14 +1567,14 @@ __device__ __forceinline__ void store_deferred(const MarchArgs& a, const RayCtx&
                                                int stride, int* sp, float* sv) {
   const ViewDesc* V = a.views + r.v;
   int32_t* nnout = a.nn_idx ? a.nn_idx[r.v] : nullptr;
-  if (nnout) nnout[((int64_t)r.i * V->nx + r.j) * V->nz + k] = o;
+  if (nnout) nnout[FOMO_IDX(((int64_t)r.i * V->nx + r.j) * V->nz + k, (int64_t)V->nx * V->ny * V->nz, kSiteNnIdx)] = o;
   if (POS) {
     *npos_at(a, r.item, k, stride) = p;
     return;
   }
   float vl = 0.0f;
   if (p >= 0 && kind == kDeferredSpectral) {
-    const float4 vv = __ldg(a.snap.vel + p);
+    const float4 vv = __ldg(a.snap.vel + FOMO_IDX(p, a.snap.n, kSitePts));
     vl = fmaf(V->uz, vv.z, fmaf(V->uy, vv.y, V->ux * vv.x));
   }
   *sp = p;
@@ -1548,7 +1606,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
     k = __shfl_sync(kFull, k, 0);
     if ((int64_t)k >= nover) return;
     const int64_t slot = a.deferred_cap - 1 - (int64_t)k;
-    const DeferredRec rec = a.deferred[slot];
+    const DeferredRec rec = a.deferred[FOMO_IDX(slot, a.deferred_cap, kSiteDeferred)];
     RayCtx r;
     if (!ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, r)) continue;  // records come from real rays only
     const ViewDesc* V = a.views + r.v;
@@ -1572,7 +1630,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       const bool done = in.act[i] && !o.need[i];
-      if (nnout && done) nnout[ray * nz + s0 + lane + 32 * i] = o.orig[i];
+      if (nnout && done) nnout[FOMO_IDX(ray * nz + s0 + lane + 32 * i, (int64_t)V->nx * V->ny * nz, kSiteNnIdx)] = o.orig[i];
       if (POS) {
         if (done) *npos_at(a, rec.x, s0 + lane + 32 * i, ktab_stride) = o.pos[i];
         continue;
@@ -1583,7 +1641,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
         const int d = n + __popc(fm & ((1u << lane) - 1u));
         float vl = 0.0f;
         if (kind == kDeferredSpectral) {
-          const float4 vv = __ldg(a.snap.vel + o.pos[i]);
+          const float4 vv = __ldg(a.snap.vel + FOMO_IDX(o.pos[i], a.snap.n, kSitePts));
           vl = fmaf(V->uz, vv.z, fmaf(V->uy, vv.y, V->ux * vv.x));
         }
         spos[w][d] = o.pos[i];
@@ -1598,7 +1656,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
     }
     const unsigned f0 = __ballot_sync(kFull, in.act[0] && o.need[0]);
     const unsigned f1 = __ballot_sync(kFull, in.act[1] && o.need[1]);
-    if (lane == 0) a.deferred[slot] = make_uint4(rec.x, rec.y, f0, f1);
+    if (lane == 0) a.deferred[FOMO_IDX(slot, a.deferred_cap, kSiteDeferred)] = make_uint4(rec.x, rec.y, f0, f1);
   }
 }
 
@@ -1634,7 +1692,7 @@ __device__ __forceinline__ void deferred_search(const MarchArgs& a, int kind, in
       if (hard) {
         const int64_t slot = (int64_t)hb + __popc(hm & ((1u << lane) - 1u));
         if (slot < a.hard_cap) {
-          a.hard[slot] = make_uint2(r.item, (unsigned)k);
+          a.hard[FOMO_IDX(slot, a.hard_cap, kSiteHard)] = make_uint2(r.item, (unsigned)k);
           p = -1;  // its neighbour and emission come from march_hard
         } else {
           lane_search_full(a.snap, exact_box(r, k), p, o);  // queue full: finish here
@@ -1743,7 +1801,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtas) march_hard(MarchArgs a, co
     if (lane == 0) i = atomicAdd(a.counter + kCtrHardHead, 1ull);
     i = __shfl_sync(kFull, i, 0);
     if ((int64_t)i >= n) return;
-    const uint2 hs = a.hard[i];
+    const uint2 hs = a.hard[FOMO_IDX(i, a.hard_cap, kSiteHard)];
     RayCtx r;
     if (!ray_of_item(a, ktab, ktab_stride, (int64_t)hs.x, r)) continue;  // queued from real rays only
     int p, o;
@@ -1845,6 +1903,8 @@ cudaError_t launch_fused_pass(const MarchArgs& a, const double3* ktab, int ktab_
 }
 
 }  // namespace
+
+FOMO_DEFINE_CHECK_READER(check_word_march)
 
 int march_bins_per_lane(int nlines, int L) {
   (void)nlines;

@@ -68,7 +68,8 @@ __global__ void __launch_bounds__(kProjThreads) projection_kernel(SnapDev snap, 
         const LineDesc& D = LD[l];
         if (!D.ew || pix < 0) continue;
         const float e = __ldg(D.ew + p).x;
-        if (e != 0.0f) atomicAdd(D.out + pix, (float)(D.is_dn ? V->scale_dn : V->scale) * e);
+        if (e != 0.0f)
+          atomicAdd(D.out + FOMO_IDX(pix, (int64_t)nx * ny, kSiteProjection), (float)(D.is_dn ? V->scale_dn : V->scale) * e);
       }
       continue;
     }
@@ -84,11 +85,11 @@ __global__ void __launch_bounds__(kProjThreads) projection_kernel(SnapDev snap, 
         const float sc = __fdividef(2.0f, pw.y);
         const float ns = -(vs * D.shift_k) * sc;
         const float scale = (float)(D.is_dn ? V->scale_dn : V->scale);
-        float* out = D.out + (int64_t)ps * L;
+        float* out = D.out + FOMO_IDX((int64_t)ps * L, (int64_t)nx * ny * L, kSiteProjection);
         for (int m = 0; m < D.nw; ++m) {
           const int il = D.wstart + 32 * m + lane;
           if (il < L) {
-            const float qq = fmaf(__ldg(D.lam + il), sc, ns);
+            const float qq = fmaf(__ldg(D.lam + FOMO_IDX(il, L, kSiteLam)), sc, ns);
             const float v = pw.x * ex2_approx(-qq * qq);
             if (v != 0.0f) atomicAdd(out + il, v * scale);
           }
@@ -99,6 +100,8 @@ __global__ void __launch_bounds__(kProjThreads) projection_kernel(SnapDev snap, 
 }
 
 }  // namespace
+
+FOMO_DEFINE_CHECK_READER(check_word_projection)
 
 cudaError_t launch_projection(SnapDev snap, const ViewDesc* views, const LineDesc* lines, int nviews, int nlines,
                               bool imaging, int sm_count, cudaStream_t s) {

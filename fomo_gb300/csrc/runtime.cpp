@@ -50,6 +50,32 @@ int cuda_err(fomo_ctx* c, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_err(ctx, e_, what); \
   } while (0)
 
+// ---------------------------------------------------------------- bounds checks
+
+// The bounds-check build (FOMO_BOUNDS_CHECK=1) records the site of the first
+// index out of range per kernel file in a device word and keeps every access
+// inside its buffer (fomo_device.cuh).  After each synchronising call the
+// words are read and cleared; a set word fails the call with FOMO_EDEVICE.
+// The regular build has no such words to read.
+int check_device_words(fomo_ctx* ctx) {
+#if defined(FOMO_BOUNDS_CHECK) && FOMO_BOUNDS_CHECK
+  static const char* const names[] = {"march", "index", "view", "emission", "projection"};
+  cudaError_t (*const readers[])(unsigned*) = {check_word_march, check_word_index, check_word_view,
+                                               check_word_emission, check_word_projection};
+  for (int k = 0; k < 5; ++k) {
+    unsigned w = 0;
+    const cudaError_t e = readers[k](&w);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "bounds-check word");
+    if (w)
+      return set_err(ctx, FOMO_EDEVICE, std::string("bounds check: index out of range in ") + names[k] +
+                                            ".cu (site " + std::to_string(w) + ")");
+  }
+#else
+  (void)ctx;
+#endif
+  return FOMO_OK;
+}
+
 // ---------------------------------------------------------------- memory
 
 int dev_alloc(fomo_ctx* ctx, void** p, size_t bytes) {
@@ -919,6 +945,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.hard = reinterpret_cast<uint2*>(db + G.o_hard);
     a.hard_cap = G.hard_cap;
     a.npos = G.o_npos ? reinterpret_cast<int32_t*>(db + G.o_npos) : nullptr;
+    a.npos_cap = G.o_npos ? G.npos_items * (int64_t)G.maxnz : 0;
     a.nn_idx = G.any_nn ? reinterpret_cast<int32_t* const*>(db + G.o_nnp) : nullptr;
     a.s2 = s2;
     a.totpol = G.totpol;
@@ -940,7 +967,10 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
       bool first = true;
       for (size_t k = 0; k + 1 < cuts.size() && e == cudaSuccess && rc == FOMO_OK; ++k) {
         const int64_t i0 = G.item_off[cuts[k]], i1 = G.item_off[cuts[k + 1]];
-        const int64_t step = G.npos_items > 0 ? G.npos_items : (i1 - i0);
+        int64_t step = G.npos_items > 0 ? G.npos_items : (i1 - i0);
+        // ranges of bounded work also split a large view's rays into launches
+        // of about range_cost, so that other streams' kernels start in between
+        if (range_cost > 0.0) step = std::min<int64_t>(step, std::max<int64_t>(1024, (int64_t)(range_cost / G.maxnz)));
         for (int64_t b = i0; b < i1 && e == cudaSuccess; b += step) {
           if (!first) e = cudaMemsetAsync(db + G.o_ctr, 0, sizeof(unsigned long long) * kCtrCount, s);
           first = false;
@@ -1116,7 +1146,7 @@ int fomo_ctx_synchronize(fomo_ctx* ctx) {
   if (!ctx) return FOMO_EINVAL;
   cudaSetDevice(ctx->device);
   FOMO_CUDA(cudaStreamSynchronize(ctx->stream), "synchronize");
-  return FOMO_OK;
+  return check_device_words(ctx);
 }
 
 int fomo_host_register(fomo_ctx* ctx, void* ptr, size_t bytes) {
@@ -1141,6 +1171,11 @@ int fomo_snapshot_create(fomo_ctx* ctx, int64_t n, const float* x, const float* 
   SnapRec r;
   int rc = build_snapshot(ctx, n, host, &r);
   if (rc) return rc;
+  rc = check_device_words(ctx);
+  if (rc) {
+    dev_free(ctx, r.block);
+    return rc;
+  }
   int nid = ctx->next_id++;
   ctx->snaps[nid] = r;
   *id = nid;
@@ -1299,6 +1334,8 @@ int fomo_render_device(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube
   if (rc) return rc;
   if (info) {
     FOMO_CUDA(cudaStreamSynchronize(s), "render");
+    rc = check_device_words(ctx);
+    if (rc) return rc;
     rc = finish_views(ctx, &views);
     if (rc) return rc;
     const TableHost* t = uses_table(req->method) ? &ctx->tables[req->table].h : nullptr;
@@ -1362,6 +1399,8 @@ int fomo_render_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* 
   const cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
   if (rc) return rc;
   FOMO_CUDA(e1 != cudaSuccess ? e1 : e2, "render");
+  rc = check_device_words(ctx);
+  if (rc) return rc;
   if (ctx->time_march) cudaEventElapsedTime(&ctx->last_ms, ctx->scratch.ev0, ctx->scratch.ev1);
   if (infos) {
     rc = finish_views(ctx, &views);
@@ -1396,6 +1435,8 @@ int fomo_render(fomo_ctx* ctx, const fomo_request* req, float* out_cube, int32_t
   if (d_nn)
     FOMO_CUDA(cudaMemcpyAsync(out_nn_idx, d_nn, nn_bytes, cudaMemcpyDeviceToHost, ctx->stream), "index download");
   FOMO_CUDA(cudaStreamSynchronize(ctx->stream), "render");
+  rc = check_device_words(ctx);
+  if (rc) return rc;
   if (ctx->time_march) cudaEventElapsedTime(&ctx->last_ms, ctx->scratch.ev0, ctx->scratch.ev1);
   if (info) {
     rc = finish_views(ctx, &views);
@@ -1423,7 +1464,7 @@ int fomo_emission(fomo_ctx* ctx, int snapshot, int table, int imaging, double ab
   FOMO_CUDA(cudaMemcpyAsync(eps, a, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream), "emission download");
   FOMO_CUDA(cudaMemcpyAsync(fwhm, b, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream), "emission download");
   FOMO_CUDA(cudaStreamSynchronize(ctx->stream), "emission");
-  return FOMO_OK;
+  return check_device_words(ctx);
 }
 
 int fomo_thomson_emission(fomo_ctx* ctx, int snapshot, float* tot, float* pol) {

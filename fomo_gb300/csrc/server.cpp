@@ -9,9 +9,12 @@
 // enqueues it on the slot's stream.  While one slot's batch runs, requests
 // that arrive meanwhile are admitted into the other slot, so their work
 // overlaps on the device.  A slot's batch marches in view ranges of bounded
-// work, launches with less work first and smaller images first within a
-// launch; each range's cubes download as soon as it is done and its requests
-// complete then, without waiting for the rest of the batch.  Results go
+// work (a large view in launches of bounded work), launches with less work
+// first and smaller images first within a launch; each range's cubes download
+// as soon as it is done and its requests complete then, without waiting for the
+// rest of the batch.  Each slot has a high- and a default-priority stream: a
+// batch of small requests only goes on the high-priority one, so its kernels
+// start ahead of a large request's next launch.  Results go
 // device -> pinned staging -> the caller's buffer; each request records
 // submit / admit / start / done times.
 //
@@ -20,6 +23,7 @@
 // arithmetic depends on what else shares the launch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -59,7 +63,9 @@ struct Ticket {
 
 struct Slot {
   ScratchSet scr;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;       // the stream of the batch in flight: one of the two below
+  cudaStream_t stream_lo = nullptr;    // default priority: batches with a large request
+  cudaStream_t stream_hi = nullptr;    // high priority: batches of small requests only
   cudaEvent_t done = nullptr;
   Arena out;              // device cubes of the batch
   char* pinned = nullptr; // host staging of the cubes
@@ -75,8 +81,13 @@ struct Slot {
 };
 
 // Work per view range of a slot's batch (LOS samples + output cells): about a
-// millisecond of march.
+// millisecond of march.  A larger view marches its rays in launches of about
+// this much work too, so that the other slot's kernels can start in between.
 constexpr double kServeRangeCost = double(1 << 24);
+// A batch whose largest request has at most this many LOS samples goes on the
+// slot's high-priority stream: its kernels are scheduled before a large
+// request's as SMs free up.
+constexpr double kServeSmallSamples = double(1 << 23);
 
 }  // namespace
 
@@ -162,6 +173,9 @@ int launch_slot(fomo_server* S, Slot& sl, std::vector<uint64_t>& ids, std::vecto
   }
   std::vector<float*> d(n);
   for (int i = 0; i < n; ++i) d[i] = reinterpret_cast<float*>(sl.out.base + doff[i]);
+  double largest = 0.0;
+  for (const fomo_request& q : reqs) largest = std::max(largest, (double)q.nx * q.ny * q.nz);
+  sl.stream = largest <= kServeSmallSamples ? sl.stream_hi : sl.stream_lo;
   Plan plan;
   rc = plan_batch(ctx, reqs.data(), n, d.data(), nullptr, &sl.scr, &plan);
   if (rc) return rc;
@@ -302,12 +316,17 @@ int fomo_server_create(const fomo_server_config* config, fomo_server** out) {
   S->budget = config->hbm_budget_bytes ? config->hbm_budget_bytes : fr / 2;
   S->max_inflight = config->max_inflight > 0 ? config->max_inflight : 64;
   for (Slot& sl : S->slots) {
-    if (sl.scr.init() != cudaSuccess || cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);  // (least, greatest): greatest is numerically lowest
+    if (sl.scr.init() != cudaSuccess ||
+        cudaStreamCreateWithPriority(&sl.stream_lo, cudaStreamNonBlocking, lo) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&sl.stream_hi, cudaStreamNonBlocking, hi) != cudaSuccess ||
         cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) {
       fomo_ctx_destroy(ctx);
       delete S;
       return FOMO_EDEVICE;
     }
+    sl.stream = sl.stream_lo;
   }
   S->t0 = now_s();
   S->worker = std::thread(scheduler, S);
@@ -390,14 +409,16 @@ int fomo_server_destroy(fomo_server* S) {
   }
   if (S->worker.joinable()) S->worker.join();
   for (Slot& sl : S->slots) {
-    if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.stream_lo) cudaStreamSynchronize(sl.stream_lo);
+    if (sl.stream_hi) cudaStreamSynchronize(sl.stream_hi);
     dev_free(S->ctx, sl.scr.arena.base);
     dev_free(S->ctx, sl.out.base);
     sl.scr.release();
     if (sl.pinned) cudaFreeHost(sl.pinned);
     for (cudaEvent_t ev : sl.evpool) cudaEventDestroy(ev);
     if (sl.done) cudaEventDestroy(sl.done);
-    if (sl.stream) cudaStreamDestroy(sl.stream);
+    if (sl.stream_lo) cudaStreamDestroy(sl.stream_lo);
+    if (sl.stream_hi) cudaStreamDestroy(sl.stream_hi);
   }
   fomo_ctx_destroy(S->ctx);
   delete S;

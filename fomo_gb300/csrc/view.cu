@@ -19,6 +19,7 @@
 #include <float.h>
 #include <stdint.h>
 
+#include "fomo_device.cuh"
 #include "fomo_internal.h"
 
 namespace fomo {
@@ -137,7 +138,7 @@ __global__ void view_extents_kernel(SnapDev snap, ViewDesc* views, float* s2) {
       double pp = __dmul_rn(xa, xa);
       pp = __dadd_rn(pp, __dmul_rn(ya, ya));
       pp = __dadd_rn(pp, __dmul_rn(za, za));
-      s2v[i] = __double2float_rn(__dsub_rn(1.0, __ddiv_rn(__dmul_rn(ip, ip), pp)));
+      s2v[FOMO_IDX(i, snap.n, kSiteS2)] = __double2float_rn(__dsub_rn(1.0, __ddiv_rn(__dmul_rn(ip, ip), pp)));
     }
     const unsigned long long ex = d2ord(xa), ey = d2ord(ya), ez = d2ord(za);
     mn[0] = ex < mn[0] ? ex : mn[0];
@@ -216,18 +217,20 @@ __global__ void view_finalize_kernel(ViewDesc* views, double3* ktab, int ktab_st
   const double dz = s_dz, minz = s_minz;
   // ray positions in the image plane (nn:152-153)
   for (int j = threadIdx.x; j < V->nx; j += blockDim.x)
-    V->xt[j] = __dadd_rn(__dmul_rn(__ddiv_rn((double)j, (double)(V->nx - 1)), V->dxr), V->minx);
+    V->xt[FOMO_IDX(j, V->nx, kSiteRayXY)] = __dadd_rn(__dmul_rn(__ddiv_rn((double)j, (double)(V->nx - 1)), V->dxr), V->minx);
   for (int i = threadIdx.x; i < V->ny; i += blockDim.x)
-    V->yt[i] = __dadd_rn(__dmul_rn(__ddiv_rn((double)i, (double)(V->ny - 1)), V->dyr), V->miny);
+    V->yt[FOMO_IDX(i, V->ny, kSiteRayXY)] = __dadd_rn(__dmul_rn(__ddiv_rn((double)i, (double)(V->ny - 1)), V->dyr), V->miny);
   double3* kt = ktab + (int64_t)blockIdx.x * ktab_stride;
   for (int k = threadIdx.x; k < V->nz; k += blockDim.x) {
     const double z = __dadd_rn(__dmul_rn((double)k, dz), minz);  // nn:162
     const double zsb = __dmul_rn(z, sb);
-    kt[k] = make_double3(__dmul_rn(zsb, cl), __dmul_rn(zsb, sl), __dmul_rn(z, cb));
+    kt[FOMO_IDX(k, ktab_stride, kSiteKtab)] = make_double3(__dmul_rn(zsb, cl), __dmul_rn(zsb, sl), __dmul_rn(z, cb));
   }
 }
 
 }  // namespace
+
+FOMO_DEFINE_CHECK_READER(check_word_view)
 
 cudaError_t launch_view_init(ViewDesc* views, int nviews, cudaStream_t s) {
   view_init_kernel<<<(nviews + 127) / 128, 128, 0, s>>>(views, nviews);
