@@ -384,8 +384,15 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     sh = ctypes_stream(stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    cache = os.path.join(ROOT, "profiles", "autotune_cache.txt")
-    ctx.autotune(reqs, cache_path=cache if os.path.exists(cache) else None)
+    # the autotuner measures its candidates on this batch and keeps the fastest;
+    # it writes its choice to a cache file, read back here for the JSON line
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        cache = os.path.join(td, "autotune.txt")
+        ctx.autotune(reqs, cache_path=cache)
+        with open(cache) as f:
+            tuned = [dict(zip(("class", "tile_w", "tile_h", "search_ctas_per_sm_cap", "gather_radius_spacings",
+                               "ms_per_batch"), ln.split())) for ln in f if ln.strip()]
 
     for _ in range(args.warmup):
         ctx.render_batch_device(reqs, ptrs, stream=sh, graph=True)
@@ -482,20 +489,25 @@ def run_ours(args):
     h2d = sum(a.numel() * 4 for a in hsnap) + sum(t.G.nbytes + t.logT.nbytes + t.logn.nbytes for t in tables)
     d2h = sum(o.numel() * 4 for o in hout)
     e2e_steps = 5  # median of 5: host-side copies vary with other jobs on the host
+    phases = []
     for k in range(e2e_steps + 1):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         s2 = ctx_snapshot_from_pinned(ctx, hsnap)
+        t1 = time.perf_counter()
         tids2 = [ctx.table(t) for t in tables]
         reqs2 = [ctx.request(s2, tid, fg.METHOD_NN, NX, NY, NZ, NL, float(ls[v]), float(bs[v]), WIDTH)
                  for v in range(NVIEWS) for tid in tids2]
+        t2 = time.perf_counter()
         cubes, _ = ctx.render_batch(reqs2, outs=[h.numpy() for h in hout])
-        dt = time.perf_counter() - t0
+        t3 = time.perf_counter()
+        dt = t3 - t0
         ctx.drop_snapshot(s2)
         for t in tids2:
             ctx.drop_table(t)
         if k > 0:
             e2e_times.append(dt)
+            phases.append((t1 - t0, t2 - t1, t3 - t2, time.perf_counter() - t3))
     e2e_med = float(np.median(e2e_times))
     e2e_value = world * line_samples / e2e_med
 
@@ -545,7 +557,11 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "line-samples/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": len(e2e_times), "stat": "median",
                     "ms_per_step": 1e3 * e2e_med, "ms_min": 1e3 * float(np.min(e2e_times)),
-                    "ms_max": 1e3 * float(np.max(e2e_times)), "ms_steps": [1e3 * t for t in e2e_times]},
+                    "ms_max": 1e3 * float(np.max(e2e_times)), "ms_steps": [1e3 * t for t in e2e_times],
+                    "ms_phases": {"snapshot_upload_and_index": [1e3 * p[0] for p in phases],
+                                  "tables": [1e3 * p[1] for p in phases],
+                                  "render_and_download": [1e3 * p[2] for p in phases],
+                                  "release_untimed": [1e3 * p[3] for p in phases]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                          "bytes_per_sample": bps,
@@ -555,6 +571,7 @@ def run_ours(args):
                                    "march_spectral<4,1,shade> (emission from the positions), timed together",
                          "binding": binding_bound(kernels)},
             "cpu_baseline": cpu,
+            "autotuned": tuned,
             "clocks": clocks,
             "ceilings": ceilings,
             "kernels": kernels,
@@ -589,9 +606,18 @@ def run_profile_case(args):
     """Small case for ncu: the batched workload cut to 8 views (268 M LOS samples,
     ~130 MB resident), issued directly (no graph), 1 warm-up + 2 launches; then
     (outside any ncu kernel filter of interest) one launch with per-kernel
-    events and one with the search counters, printed as JSON."""
+    events and one with the search counters, printed as JSON.
+
+    --tune-cache PATH: the march configuration of the autotuner's cache file at
+    PATH; when PATH does not exist yet, the autotuner first measures its
+    candidates on this batch and writes it (run once without ncu, so that a
+    capture that follows contains no tuning launches)."""
     import fomo_gb300 as fg
     snap, tables, ls, bs = make_workload()
+    tuned = None
+    if args.tune_cache and os.path.exists(args.tune_cache):
+        os.environ["FOMO_TUNE_CACHE"] = args.tune_cache
+        tuned = open(args.tune_cache).read().split()
     with fg.Context(0) as ctx:
         sid = ctx.snapshot(snap)
         tids = [ctx.table(t) for t in tables]
@@ -602,6 +628,9 @@ def run_profile_case(args):
         dev = torch.device("cuda", 0)
         outs = [torch.empty((NY, NX, NL), dtype=torch.float32, device=dev) for _ in reqs]
         ptrs = [o.data_ptr() for o in outs]
+        if args.tune_cache and tuned is None:
+            ctx.autotune(reqs, cache_path=args.tune_cache)
+            tuned = open(args.tune_cache).read().split()
         for _ in range(3):
             ctx.render_batch_device(reqs, ptrs)
             ms = ctx.last_march_ms()
@@ -617,7 +646,7 @@ def run_profile_case(args):
             ctx.set_profiling(False, False)
         print(json.dumps({"profile_case": f"{nv} views x {len(tables)} lines, {NX}x{NY}x{NZ}, L={NL}",
                           "march_ms": ms, "los_samples": nv * NX * NY * NZ, "kernel_ms": kernel_ms,
-                          "counters": counters}))
+                          "counters": counters, "tuned": tuned}))
 
 
 def main():
@@ -630,6 +659,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (mixed request stream) leg")
     ap.add_argument("--profile-case", action="store_true", help="small direct-launch case for ncu captures")
     ap.add_argument("--no-breakdown", action="store_true", help="profile case without the timing/counter launches")
+    ap.add_argument("--tune-cache", default=None, help="profile case: autotuner cache file (written when absent)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -102,6 +102,11 @@ SIGNATURES = {
     "fomo_abundance_ratio": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                              ctypes.POINTER(ctypes.c_double)],
     "fomo_snapshot_get_info": [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(SnapshotInfo)],
+    "fomo_snapshot_from_amrvac": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_int)],
+    "fomo_amrvac_points": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                           ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int64,
+                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int)] + [_F] * 8,
     "fomo_table_create": [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_char_p,
                           ctypes.c_int, ctypes.c_int, _F, _F, _F, ctypes.POINTER(ctypes.c_int)],
     "fomo_table_load": [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)],
@@ -223,6 +228,29 @@ class Context:
         self._check(self._L.fomo_snapshot_create_device(self.h, n, *[ctypes.c_void_p(p) if p else None for p in ptrs],
                                                         ctypes.byref(sid)))
         return sid.value
+
+    def snapshot_from_amrvac(self, datfile: str, amrvacpar: str | None = None, amrvac_version: str = "gitlab",
+                             gamma_eqparposition: int = 0, n_unit: float = 1.0, Teunit: float = 1.0,
+                             L_unit: float = 1.0) -> int:
+        """A snapshot read from an AMRVAC data file (fomo_snapshot_from_amrvac)."""
+        sid = ctypes.c_int()
+        self._check(self._L.fomo_snapshot_from_amrvac(self.h, datfile.encode(),
+                                                      amrvacpar.encode() if amrvacpar else None,
+                                                      amrvac_version.encode(), gamma_eqparposition, n_unit, Teunit,
+                                                      L_unit, ctypes.byref(sid)))
+        return sid.value
+
+    def amrvac_points(self, datfile: str, amrvacpar: str | None = None, amrvac_version: str = "gitlab",
+                      gamma_eqparposition: int = 0, n_unit: float = 1.0, Teunit: float = 1.0, L_unit: float = 1.0):
+        """(ndim, [x, y, z, n, T, vx, vy, vz]) of an AMRVAC data file, in the reference's point order."""
+        args = (self.h, datfile.encode(), amrvacpar.encode() if amrvacpar else None, amrvac_version.encode(),
+                gamma_eqparposition, n_unit, Teunit, L_unit)
+        n, nd = ctypes.c_int64(), ctypes.c_int()
+        self._check(self._L.fomo_amrvac_points(*args, 0, ctypes.byref(n), ctypes.byref(nd), *([None] * 8)))
+        arrs = [np.empty(n.value, np.float32) for _ in range(8)]
+        self._check(self._L.fomo_amrvac_points(*args, n.value, ctypes.byref(n), ctypes.byref(nd),
+                                               *[_fp(a) for a in arrs]))
+        return nd.value, arrs
 
     def snapshot_info(self, sid: int) -> SnapshotInfo:
         info = SnapshotInfo()

@@ -28,7 +28,7 @@ std::string plan_key(const Plan& p, const ScratchSet& scr) {
   for (const PlanGroup& G : p.groups)
     k << "|" << G.snapshot << "," << G.method << "," << G.imaging << "," << G.nv << "," << G.nl << "," << G.maxL
       << "," << G.maxnz << "," << G.maxnx << "," << G.maxny << "," << G.total_items << "," << G.tw << "," << G.th
-      << "," << G.bps << "," << G.any_nn << "," << (const void*)G.totpol;
+      << "," << G.bps << "," << G.rscale << "," << G.any_nn << "," << (const void*)G.totpol;
   return k.str();
 }
 
@@ -89,8 +89,16 @@ int fomo_render_batch_graph(fomo_ctx* ctx, const fomo_request* reqs, int nreq, f
   return FOMO_OK;
 }
 
-// Measure candidate ray tiles / CTA caps on the given batch (device outputs),
-// keep the fastest per workload class.  Cache file lines: "<class> tw th bps ms".
+// Measure candidate march configurations on the given batch (device
+// outputs), keep the fastest per workload class.  The axes: the ray tile
+// (which rays a warp takes one after the other, i.e. the L1/L2 locality of
+// consecutive work items), the CTAs-per-SM cap of the search pass (its
+// occupancy against its shared-memory candidate lists), and the gather radius
+// of the search in local point spacings (a wider gather resolves more samples
+// in the first pass, at more candidates per segment; a narrower one leaves more
+// to the deferred pass).  The segment length is fixed at 64 LOS samples (two
+// per lane) by the deferred-record format.  Cache file lines:
+// "<class> tile_w tile_h blocks_per_sm rscale ms".
 int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char* cache_path) {
   if (!ctx || !reqs || nreq <= 0) return FOMO_EINVAL;
   cudaSetDevice(ctx->device);
@@ -119,11 +127,9 @@ int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char*
     bool all = true;
     std::map<std::string, TuneChoice> found;
     while (std::getline(f, line)) {
-      std::istringstream ls(line);
       std::string k;
       TuneChoice c;
-      double ms;
-      if (ls >> k >> c.tile_w >> c.tile_h >> c.blocks_per_sm >> ms) found[k] = c;
+      if (parse_tune_line(line, &k, &c)) found[k] = c;
     }
     for (auto& k : classes) {
       if (found.count(k))
@@ -134,7 +140,11 @@ int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char*
     if (all) return FOMO_OK;
   }
   const int saved_w = ctx->tile_w, saved_h = ctx->tile_h, saved_b = ctx->blocks_per_sm;
-  const int cands[][3] = {{8, 4, 0}, {16, 2, 0}, {4, 8, 0}, {32, 1, 0}, {16, 4, 0}, {8, 8, 0}, {8, 4, 2}, {8, 4, 1}};
+  const float saved_r = ctx->rscale;
+  // {tile_w, tile_h, CTA cap of the search, gather radius x 10}: tiles at the
+  // default search, then the search's occupancy and radius at the default tile
+  const int cands[][4] = {{8, 4, 0, 9},  {16, 2, 0, 9}, {4, 8, 0, 9},  {32, 1, 0, 9},  {8, 8, 0, 9},
+                          {8, 4, 6, 9},  {8, 4, 5, 9},  {8, 4, 0, 8},  {8, 4, 0, 10}, {8, 4, 0, 11}};
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -144,6 +154,7 @@ int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char*
     ctx->tile_w = c[0];
     ctx->tile_h = c[1];
     ctx->blocks_per_sm = c[2];
+    ctx->rscale = 0.1f * (float)c[3];
     rc = enqueue_batch(ctx, reqs, nreq, d.data(), nullptr, ctx->stream, nullptr, nullptr);  // warm-up
     if (rc) break;
     cudaEventRecord(e0, ctx->stream);
@@ -159,7 +170,7 @@ int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char*
     cudaEventElapsedTime(&ms, e0, e1);
     if (ms < best) {
       best = ms;
-      bestc = TuneChoice{c[0], c[1], c[2]};
+      bestc = TuneChoice{c[0], c[1], c[2], 0.1f * (float)c[3]};
     }
   }
   cudaEventDestroy(e0);
@@ -167,12 +178,14 @@ int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char*
   ctx->tile_w = saved_w;
   ctx->tile_h = saved_h;
   ctx->blocks_per_sm = saved_b;
+  ctx->rscale = saved_r;
   if (rc) return rc;
   for (auto& k : classes) ctx->tuned[k] = bestc;
   if (cache_path) {
     std::ofstream f(cache_path, std::ios::app);
     for (auto& k : classes)
-      f << k << " " << bestc.tile_w << " " << bestc.tile_h << " " << bestc.blocks_per_sm << " " << best / 2 << "\n";
+      f << k << " " << bestc.tile_w << " " << bestc.tile_h << " " << bestc.blocks_per_sm << " " << bestc.rscale << " "
+        << best / 2 << "\n";
   }
   return FOMO_OK;
 }

@@ -110,7 +110,7 @@ struct MarchArgs {
   int64_t npos_cap;              // its entries (index checks of the bounds-check build)
   const float* s2;               // Thomson: per-view sin^2(chi) per sorted point (nviews * n), else null
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
-  unsigned int* err;             // device error word (bounds-check builds)
+  float rscale;                  // gather radius of the search in local point spacings (0: the default, 0.9)
   unsigned long long* stats;     // optional search counters (profiling), else null
 };
 
@@ -205,6 +205,7 @@ cudaError_t check_word_index(unsigned* out);
 cudaError_t check_word_view(unsigned* out);
 cudaError_t check_word_emission(unsigned* out);
 cudaError_t check_word_projection(unsigned* out);
+cudaError_t check_word_amrvac(unsigned* out);
 
 // march.cu
 // The march: the first search pass and the emission sums of every ray, then

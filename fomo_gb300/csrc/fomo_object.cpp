@@ -26,6 +26,7 @@
 #include <sstream>
 #include <stdexcept>
 
+#include "../../include/FoMo-amrvac.h"
 #include "../../include/FoMo.h"
 #include "../../include/fomo_gpu.h"
 #include "fomo_consts.h"
@@ -650,3 +651,55 @@ void FoMoObject::render(const std::vector<double> lvec, const std::vector<double
 }
 
 }  // namespace FoMo
+
+// ---------------------------------------------------------------- AMRVAC
+
+void read_amrvac_par_file(const char* amrvacpar, const int ndim, std::vector<int>& nxlone,
+                          std::vector<double>& xprobmin, std::vector<double>& xprobmax) {
+  std::ifstream in(amrvacpar ? amrvacpar : "");
+  if (!in) throw std::runtime_error(std::string("amrvac.par file not found at ") + (amrvacpar ? amrvacpar : "(null)"));
+  std::stringstream ss;
+  ss << in.rdbuf();
+  const std::string text = ss.str();
+  nxlone.assign(ndim, 0);
+  xprobmin.assign(ndim, 0.0);
+  xprobmax.assign(ndim, 0.0);
+  const char* keys[3] = {"nxlone", "xprobmin", "xprobmax"};
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < ndim; ++i) {
+      const std::string key = keys[j] + std::to_string(i + 1);
+      const size_t at = text.find(key);
+      const size_t start = at == std::string::npos ? at : text.find_first_of("\t\n= ", at + 1);
+      if (start == std::string::npos)
+        throw std::runtime_error(std::string(amrvacpar) + " does not contain the key " + key);
+      const char* v = text.c_str() + start + 1;
+      if (j == 0) nxlone[i] = std::atoi(v);
+      if (j == 1) xprobmin[i] = std::strtod(v, nullptr);
+      if (j == 2) xprobmax[i] = std::strtod(v, nullptr);
+    }
+}
+
+FoMo::FoMoObject read_amrvac_dat_file(const char* datfile, const char* amrvacpar, std::string amrvac_version,
+                                      const int gamma_eqparposition, const double n_unit, const double Teunit,
+                                      const double L_unit) {
+  fomo_ctx* ctx = FoMo::shared_context();
+  int64_t n = 0;
+  int ndim = 0;
+  FoMo::check(ctx,
+        fomo_amrvac_points(ctx, datfile, amrvacpar, amrvac_version.c_str(), gamma_eqparposition, n_unit, Teunit,
+                           L_unit, 0, &n, &ndim, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                           nullptr),
+        "AMRVAC reader");
+  FoMo::tgrid grid(ndim, FoMo::tcoord((size_t)n));
+  FoMo::tvars vars(5, FoMo::tphysvar((size_t)n));
+  std::vector<float> zeros(ndim == 2 ? (size_t)n : 0);
+  FoMo::check(ctx,
+        fomo_amrvac_points(ctx, datfile, amrvacpar, amrvac_version.c_str(), gamma_eqparposition, n_unit, Teunit,
+                           L_unit, n, &n, &ndim, grid[0].data(), grid[1].data(),
+                           ndim == 3 ? grid[2].data() : zeros.data(), vars[0].data(), vars[1].data(), vars[2].data(),
+                           vars[3].data(), vars[4].data()),
+        "AMRVAC reader");
+  FoMo::FoMoObject object;
+  object.setdata(grid, vars);
+  return object;
+}

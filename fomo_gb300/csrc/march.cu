@@ -86,7 +86,7 @@ constexpr float kCellMargin = 0.02f;  // cell-boundary slack in cells (binning e
 constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
 constexpr int kSegCap = 176;          // candidates per segment (sized so that 7 search CTAs fit an SM)
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule beyond which it is deferred
-constexpr float kRScale = 0.9f;       // gather radius in local point spacings
+constexpr float kRScaleDefault = 0.9f;  // gather radius in local point spacings (MarchArgs::rscale when set)
 
 
 struct __align__(16) SegSmem {
@@ -358,7 +358,7 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
     }
     const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
     const float aloc = g.h * spacing_cells(mocc);
-    const float R = fminf(r.mdf * 1.7321f * 1.0001f, kRScale * aloc);
+    const float R = fminf(r.mdf * 1.7321f * 1.0001f, (a.rscale > 0.0f ? a.rscale : kRScaleDefault) * aloc);
     const float amax =
         fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
     const float Rg = R * 1.0001f + amax * 2.4e-7f;  // + a few ulp of the coordinates
@@ -636,7 +636,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
   }
   const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
   const float aloc = g.h * spacing_cells(mocc);
-  const float R = fminf(r.mdf * 1.7321f * 1.0001f, kRScale * aloc);
+  const float R = fminf(r.mdf * 1.7321f * 1.0001f, (a.rscale > 0.0f ? a.rscale : kRScaleDefault) * aloc);
   const float amax =
       fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
   const float Rg = R * 1.0001f + amax * 2.4e-7f;  // + a few ulp of the coordinates

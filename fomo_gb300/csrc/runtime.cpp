@@ -59,10 +59,10 @@ int cuda_err(fomo_ctx* c, cudaError_t e, const char* what) {
 // The regular build has no such words to read.
 int check_device_words(fomo_ctx* ctx) {
 #if defined(FOMO_BOUNDS_CHECK) && FOMO_BOUNDS_CHECK
-  static const char* const names[] = {"march", "index", "view", "emission", "projection"};
+  static const char* const names[] = {"march", "index", "view", "emission", "projection", "amrvac"};
   cudaError_t (*const readers[])(unsigned*) = {check_word_march, check_word_index, check_word_view,
-                                               check_word_emission, check_word_projection};
-  for (int k = 0; k < 5; ++k) {
+                                               check_word_emission, check_word_projection, check_word_amrvac};
+  for (int k = 0; k < 6; ++k) {
     unsigned w = 0;
     const cudaError_t e = readers[k](&w);
     if (e != cudaSuccess) return cuda_err(ctx, e, "bounds-check word");
@@ -734,6 +734,7 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     G.tw = ctx->tile_w;
     G.th = ctx->tile_h;
     G.bps = ctx->blocks_per_sm;
+    G.rscale = ctx->rscale;
     if (G.tw <= 0 || G.th <= 0) {
       G.tw = 8;
       G.th = 4;
@@ -742,6 +743,7 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
         G.tw = t->second.tile_w;
         G.th = t->second.tile_h;
         if (ctx->blocks_per_sm == 0) G.bps = t->second.blocks_per_sm;
+        if (ctx->rscale == 0.0f) G.rscale = t->second.rscale;
       }
     }
     G.o_views = L.take(sizeof(ViewDesc) * G.nv);
@@ -950,6 +952,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.s2 = s2;
     a.totpol = G.totpol;
     a.stats = ctx->march_stats;
+    a.rscale = G.rscale;
     if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = record_timing(scr->ev0);
     MarchTimer* timer = (ctx->kernel_timing && !capturing) ? &ctx->timer : nullptr;
     int rc = FOMO_OK;
@@ -1011,15 +1014,29 @@ int enqueue_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* cons
   return FOMO_OK;
 }
 
+// A line of the autotuner's cache file: "<class> tile_w tile_h blocks_per_sm
+// rscale ms" (lines without rscale, from before it was tuned, keep the default).
+bool parse_tune_line(const std::string& line, std::string* key, TuneChoice* c) {
+  std::istringstream ls(line);
+  std::vector<double> v;
+  if (!(ls >> *key)) return false;
+  double x;
+  while (ls >> x) v.push_back(x);
+  if (v.size() != 4 && v.size() != 5) return false;
+  c->tile_w = (int)v[0];
+  c->tile_h = (int)v[1];
+  c->blocks_per_sm = (int)v[2];
+  c->rscale = v.size() == 5 ? (float)v[3] : 0.0f;
+  return c->tile_w > 0 && c->tile_h > 0 && c->blocks_per_sm >= 0 && c->rscale >= 0.0f;
+}
+
 void load_tune_cache(fomo_ctx* ctx, const char* path) {
   std::ifstream f(path);
   std::string line;
   while (std::getline(f, line)) {
-    std::istringstream ls(line);
     std::string k;
     TuneChoice c;
-    double ms;
-    if (ls >> k >> c.tile_w >> c.tile_h >> c.blocks_per_sm >> ms) ctx->tuned[k] = c;
+    if (parse_tune_line(line, &k, &c)) ctx->tuned[k] = c;
   }
 }
 

@@ -90,6 +90,7 @@ struct PlanGroup {
   int nv = 0, nl = 1, maxL = 1, maxnz = 1, maxnx = 2, maxny = 2;
   int max_nw = 1;  // largest number of 32-bin lambda windows of a line
   int tw = 8, th = 4, bps = 0;
+  float rscale = 0.0f;
   std::vector<const float2*> ew;       // payload per request (NN)
   const float2* totpol = nullptr;      // Thomson payload
   bool any_nn = false;
@@ -126,8 +127,12 @@ struct GraphRec {
   cudaGraphExec_t exec = nullptr;
 };
 
+// One autotuned march configuration: ray tile, CTAs-per-SM cap of the search
+// pass (0 = occupancy maximum), gather radius in local point spacings (0 = the
+// default).
 struct TuneChoice {
   int tile_w = 8, tile_h = 4, blocks_per_sm = 0;
+  float rscale = 0.0f;
 };
 
 }  // namespace fomo
@@ -158,6 +163,7 @@ struct fomo_ctx {
   long fail_alloc_at = 0;  // FOMO_INJECT_ALLOC_FAILURE: this allocation (1-based) fails, for error-path tests
   long alloc_count = 0;
   int tile_w = 0, tile_h = 0, blocks_per_sm = 0;
+  float rscale = 0.0f;  // forced gather radius (autotuner trials), 0 = tuned or default
   bool time_march = true;
   float last_ms = 0.0f;
   cudaEvent_t order_ev = nullptr;  // orders a caller stream after the context stream
@@ -199,5 +205,12 @@ void fill_view_host(const fomo_request& q, double lambda0, int tw, int th, ViewD
 int finish_views(fomo_ctx* ctx, std::vector<ViewDesc>* views);
 void view_info_from(const ViewDesc& V, const fomo_request& q, const TableHost* t, fomo_view_info* info);
 int parse_table_text(const std::string& text, TableHost* t, std::string* err);
+bool parse_tune_line(const std::string& line, std::string* key, TuneChoice* c);
+// Upload n points (host or device arrays: x, y, z, n, T, vx, vy, vz; z may be
+// null) and build the snapshot's spatial index.
+int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec* out);
+// Bounds-check build: read and clear the kernels' error words (FOMO_EDEVICE
+// when one is set); FOMO_OK in the regular build.
+int check_device_words(fomo_ctx* ctx);
 
 }  // namespace fomo

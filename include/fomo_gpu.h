@@ -95,6 +95,29 @@ int fomo_snapshot_create_device(fomo_ctx* ctx, int64_t n, const float* x, const 
                                 const float* n_e, const float* T, const float* vx, const float* vy, const float* vz,
                                 int* id);
 
+/* ---- AMRVAC snapshots: replaces read_amrvac_dat_file (fomo-c/example/
+ * example_mpi_amrvac/read_amrvac_files.cpp:685-715) and the FoMoObject it
+ * fills point by point (fomo_from_amrvac, :228-299).  The data file's header,
+ * tree and leaf blocks are parsed on the host; every cell's position and
+ * primitive variables (n = rho n_unit, T = p / rho Teunit, v = m / rho V_unit
+ * with V_unit = sqrt(2 k_B Teunit / m_p)) are computed on the device in the
+ * reference's FP64 order and rounded to FP32 as its DataCube stores them; then
+ * the snapshot is built as fomo_snapshot_create does.  Version 3 and 4 files
+ * carry their own domain (amrvacpar may be NULL); older files need the
+ * amrvac.par file, amrvac_version "old" (level-1 blocks x fastest) or
+ * "gitlab" (Morton order), and gamma_eqparposition (the index of gamma among
+ * the equation parameters).  L_unit: Mm per code length.  2-D data get z = 0. */
+int fomo_snapshot_from_amrvac(fomo_ctx* ctx, const char* datfile, const char* amrvacpar, const char* amrvac_version,
+                              int gamma_eqparposition, double n_unit, double Teunit, double L_unit, int* id);
+/* The same conversion into caller host arrays of cap floats each (x, y, z,
+ * n_e, T, vx, vy, vz in the reference's point order); x == NULL only returns
+ * *npoints and *ndim.  It serves the C++ read_amrvac_dat_file of
+ * include/FoMo-amrvac.h. */
+int fomo_amrvac_points(fomo_ctx* ctx, const char* datfile, const char* amrvacpar, const char* amrvac_version,
+                       int gamma_eqparposition, double n_unit, double Teunit, double L_unit, int64_t cap,
+                       int64_t* npoints, int* ndim, float* x, float* y, float* z, float* n_e, float* T, float* vx,
+                       float* vy, float* vz);
+
 typedef struct {
   int64_t npoints;
   int grid_dims[3];

@@ -290,3 +290,41 @@ def abundance_ratio(abund_file: str, standard_file: str, ion: str) -> float:
             raise ValueError(f"invalid abundance file {path}")
         return 10.0 ** (el - h)
     return rel(abund_file) / rel(standard_file)
+
+
+def amrvac_read(datfile: str, parfile: str | None = None, amrvac_version: str = "gitlab", gamma_eqparposition: int = 0,
+                n_unit: float = 1.0, Teunit: float = 1.0, L_unit: float = 1.0):
+    """Restatement of the reference's AMRVAC reader (fo_amrvac_read): (ndim,
+    [x, y, z, n, T, vx, vy, vz]) as float32 arrays in the reference's point
+    order; z is zero for 2-D data."""
+    L = lib()
+    L.fo_amrvac_read.restype = ctypes.c_int
+    nd, npts = ctypes.c_int(), ctypes.c_long()
+    args = [datfile.encode(), parfile.encode() if parfile else None, int(amrvac_version == "gitlab"),
+            int(gamma_eqparposition), ctypes.c_double(n_unit), ctypes.c_double(Teunit), ctypes.c_double(L_unit)]
+    rc = L.fo_amrvac_read(*args, ctypes.c_long(0), ctypes.byref(nd), ctypes.byref(npts), *([None] * 8))
+    if rc not in (0, -3):
+        raise RuntimeError(f"fo_amrvac_read({datfile}) failed: {rc}")
+    arrs = [np.zeros(npts.value, np.float32) for _ in range(8)]
+    rc = L.fo_amrvac_read(*args, ctypes.c_long(npts.value), ctypes.byref(nd), ctypes.byref(npts),
+                          *[_fp(a) for a in arrs])
+    if rc != 0:
+        raise RuntimeError(f"fo_amrvac_read({datfile}) failed: {rc}")
+    return nd.value, arrs
+
+
+def ref_amrvac_read(datfile: str, parfile: str | None, amrvac_version: str, gamma_eqparposition: int,
+                    n_unit: float, Teunit: float, L_unit: float, cap: int = 1 << 22):
+    """The reference's own AMRVAC reader (read_amrvac_dat_file, compiled from its
+    sources into oracle/_ref): (ndim, [x, y, z, n, T, vx, vy, vz])."""
+    R = ref()
+    R.ref_amrvac_read.restype = ctypes.c_int
+    nd, npts = ctypes.c_int(), ctypes.c_long()
+    arrs = [np.zeros(cap, np.float32) for _ in range(8)]
+    rc = R.ref_amrvac_read(datfile.encode(), (parfile or "").encode(), amrvac_version.encode(),
+                           int(gamma_eqparposition), ctypes.c_double(n_unit), ctypes.c_double(Teunit),
+                           ctypes.c_double(L_unit), ctypes.c_long(cap), ctypes.byref(nd), ctypes.byref(npts),
+                           *[_fp(a) for a in arrs])
+    if rc != 0:
+        raise RuntimeError(f"ref_amrvac_read failed: {rc} {R.ref_last_error().decode()}")
+    return nd.value, [a[:npts.value].copy() for a in arrs]

@@ -816,3 +816,305 @@ int fo_projection_render(long n, const float* x, const float* y, const float* z,
   free(losvel);
   return FO_OK;
 }
+
+/* ------------------------------------------------------------------------- */
+/* AMRVAC snapshot reader (fomo-c/example/example_mpi_amrvac/                */
+/* read_amrvac_files.cpp), restated: the data file's header, tree ("forest") */
+/* and leaf blocks, the leaves' order, and each cell's position and          */
+/* primitive variables, with the reference's FP64 expressions and their      */
+/* rounding to FP32 when pushed into the DataCube.                           */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+  int level, idx[3];
+} fo_leaf;
+
+/* mortonEncode_for (FoMo-amrvac.h:13-19): bit i of x, y, z to bits 3i, 3i+1, 3i+2. */
+static uint64_t fo_morton3(unsigned x, unsigned y, unsigned z) {
+  uint64_t r = 0;
+  for (int i = 0; i < 21; ++i)
+    r |= ((uint64_t)((x >> i) & 1u) << (3 * i)) | ((uint64_t)((y >> i) & 1u) << (3 * i + 1)) |
+         ((uint64_t)((z >> i) & 1u) << (3 * i + 2));
+  return r;
+}
+
+/* loopthroughleafs (read_amrvac_files.cpp:20-44): depth first through the
+ * tree; a leaf is recorded with its level and 1-based index at that level. */
+static int fo_leaves(const int* forest, long nforest, long* pos, int level, int ndim, const int idx[3],
+                     fo_leaf* out, long* nout, long cap) {
+  ++*pos;
+  if (*pos >= nforest) return FO_ETABLE;
+  if (forest[*pos]) {
+    if (*nout >= cap) return FO_ECAP;
+    out[*nout].level = level;
+    out[*nout].idx[0] = idx[0];
+    out[*nout].idx[1] = idx[1];
+    out[*nout].idx[2] = idx[2];
+    ++*nout;
+    return FO_OK;
+  }
+  for (int i = 0; i < (1 << ndim); ++i) {
+    int ni[3];
+    ni[0] = 2 * (idx[0] - 1) + 1 + i % 2;
+    if (ndim == 2) {
+      ni[1] = 2 * (idx[1] - 1) + 1 + i / 2;
+      ni[2] = 1;
+    } else {
+      ni[1] = 2 * (idx[1] - 1) + 1 + (i / 2) % 2;
+      ni[2] = 2 * (idx[2] - 1) + 1 + i / 4;
+    }
+    const int rc = fo_leaves(forest, nforest, pos, level + 1, ndim, ni, out, nout, cap);
+    if (rc) return rc;
+  }
+  return FO_OK;
+}
+
+typedef struct {
+  uint64_t code;
+  int i, j, k;
+} fo_mblock;
+
+static int fo_mblock_cmp(const void* a, const void* b) {
+  const uint64_t x = ((const fo_mblock*)a)->code, y = ((const fo_mblock*)b)->code;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* read_amrvac_par_file (read_amrvac_files.cpp:50-112): the first occurrence of
+ * "nxlone<d>", "xprobmin<d>", "xprobmax<d>"; the value starts after the next
+ * tab, newline, '=' or blank. */
+static int fo_par_value(const char* text, const char* key, double* v) {
+  const char* p = strstr(text, key);
+  if (!p) return FO_ETABLE;
+  p = strpbrk(p + 1, "\t\n= ");
+  if (!p) return FO_ETABLE;
+  *v = strtod(p + 1, NULL);
+  return FO_OK;
+}
+
+static int fo_read_file(const char* path, unsigned char** buf, long* size) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return FO_ENOFILE;
+  fseek(f, 0, SEEK_END);
+  *size = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  *buf = (unsigned char*)malloc(*size > 0 ? (size_t)*size : 1);
+  const size_t got = fread(*buf, 1, (size_t)*size, f);
+  fclose(f);
+  if ((long)got != *size) {
+    free(*buf);
+    return FO_ENOFILE;
+  }
+  return FO_OK;
+}
+
+
+
+int fo_amrvac_read(const char* datfile, const char* parfile, int gitlab_order, int gamma_eqparposition,
+                   double n_unit, double Teunit, double L_unit, long cap, int* ndim_out, long* npts_out, float* x,
+                   float* y, float* z, float* n, float* T, float* vx, float* vy, float* vz) {
+  unsigned char* buf = NULL;
+  long size = 0;
+  int rc = fo_read_file(datfile, &buf, &size);
+  if (rc) return rc;
+  int version, nw, ndim, nleafs, nparents = 0, neqpar;
+  int nx[3] = {1, 1, 1}, nxlone[3] = {1, 1, 1};
+  double xprobmin[3] = {0, 0, 0}, xprobmax[3] = {0, 0, 0}, gamma = 0.0;
+  long treeoff = 0, blockoff = 0, nforest = 0;
+  int ghosts = 0;
+  memcpy(&version, buf, 4);
+  if (version == 3 || version == 4) {
+    /* read_amrvac_new_dat_file (:430-528) / read_amrvac_dat_file_v4 (:535-683) */
+    int hdr[11];
+    memcpy(hdr, buf, sizeof(hdr));
+    treeoff = hdr[1];
+    blockoff = hdr[2];
+    nw = hdr[3];
+    ndim = hdr[5];
+    nleafs = hdr[7];
+    nparents = hdr[8];
+    long off = 10 * 4 + 8; /* version .. it, then t */
+    if (ndim < 2 || ndim > 3) {
+      free(buf);
+      return FO_EARG;
+    }
+    memcpy(xprobmin, buf + off, 8 * ndim);
+    off += 8 * ndim;
+    memcpy(xprobmax, buf + off, 8 * ndim);
+    off += 8 * ndim;
+    memcpy(nxlone, buf + off, 4 * ndim);
+    off += 4 * ndim;
+    memcpy(nx, buf + off, 4 * ndim);
+    off += 4 * ndim;
+    off += 16 * nw + 16; /* variable names, physics module */
+    memcpy(&neqpar, buf + off, 4);
+    off += 4;
+    const double* eq = (const double*)(buf + off);
+    double eqv;
+    for (int i = 0; i < neqpar; ++i) {
+      memcpy(&eqv, buf + off + 8 * i, 8);
+      const char* name = (const char*)(buf + off + 8 * neqpar + 16 * i);
+      /* version 3: the whole 16-byte name is "gamma" (blank or NUL padded);
+       * version 4: its first 5 characters (:503-511, :637-646) */
+      int len = 16;
+      while (len > 0 && (name[len - 1] == ' ' || name[len - 1] == '\0')) --len;
+      if ((version == 3 && len == 5 && memcmp(name, "gamma", 5) == 0) ||
+          (version == 4 && memcmp(name, "gamma", 5) == 0))
+        gamma = eqv;
+    }
+    (void)eq;
+    if (gamma == 0.0) {
+      free(buf);
+      return FO_ETABLE; /* "No value for gamma found" */
+    }
+    nforest = nparents + nleafs;
+    ghosts = 1; /* two ghost-cell counts per dimension before each block (:159-177) */
+  } else {
+    /* read_amrvac_old_dat_file (:301-418): the header at the end of the file */
+    int tail[7];
+    memcpy(tail, buf + size - 8 - 7 * 4, sizeof(tail));
+    nleafs = tail[0];
+    ndim = tail[2];
+    nw = tail[4];
+    neqpar = tail[5];
+    if (ndim < 2 || ndim > 3) {
+      free(buf);
+      return FO_EARG;
+    }
+    const long eqoff = size - 8 - 7 * 4 - 8L * neqpar;
+    const long nxoff = eqoff - 4L * ndim;
+    memcpy(nx, buf + nxoff, 4 * ndim);
+    double eqv;
+    memcpy(&eqv, buf + eqoff + 8L * gamma_eqparposition, 8);
+    gamma = eqv;
+    long nglev = (long)nx[0] * nx[1] * (ndim == 3 ? nx[2] : 1);
+    blockoff = 0;
+    treeoff = (long)nleafs * nw * nglev * 8;
+    nforest = (nxoff - treeoff) / 4;
+    /* nxlone, xprobmin, xprobmax from the amrvac.par file */
+    unsigned char* par = NULL;
+    long psize = 0;
+    rc = fo_read_file(parfile, &par, &psize);
+    if (rc) {
+      free(buf);
+      return rc;
+    }
+    char* text = (char*)malloc((size_t)psize + 1);
+    memcpy(text, par, (size_t)psize);
+    text[psize] = 0;
+    free(par);
+    const char* keys[3] = {"nxlone", "xprobmin", "xprobmax"};
+    for (int j = 0; j < 3 && !rc; ++j)
+      for (int i = 0; i < ndim && !rc; ++i) {
+        char key[32];
+        snprintf(key, sizeof(key), "%s%d", keys[j], i + 1);
+        double v = 0;
+        rc = fo_par_value(text, key, &v);
+        if (j == 0) nxlone[i] = (int)v;
+        if (j == 1) xprobmin[i] = v;
+        if (j == 2) xprobmax[i] = v;
+      }
+    free(text);
+    if (rc) {
+      free(buf);
+      return rc;
+    }
+  }
+  const long nglev1 = (long)nx[0] * nx[1] * (ndim == 3 ? nx[2] : 1);
+  /* blocksandsize (:114-129) */
+  int nblocks[3] = {1, 1, 1};
+  double cellsize[3] = {0, 0, 0};
+  for (int i = 0; i < ndim; ++i) {
+    if (nxlone[i] % nx[i] != 0) {
+      free(buf);
+      return FO_ETABLE; /* "Non-integer number of blocks" */
+    }
+    nblocks[i] = nxlone[i] / nx[i];
+    cellsize[i] = (xprobmax[i] - xprobmin[i]) / nxlone[i];
+  }
+  int* forest = (int*)malloc(sizeof(int) * (size_t)(nforest > 0 ? nforest : 1));
+  memcpy(forest, buf + treeoff, 4 * (size_t)nforest);
+  fo_leaf* leaves = (fo_leaf*)malloc(sizeof(fo_leaf) * (size_t)(nleafs > 0 ? nleafs : 1));
+  long nl = 0, pos = -1;
+  if (version != 3 && version != 4 && !gitlab_order) {
+    /* the pre-2017 order: level-1 blocks with x fastest (:380-390) */
+    for (int k = 0; k < nblocks[2] && !rc; ++k)
+      for (int j = 0; j < nblocks[1] && !rc; ++j)
+        for (int i = 0; i < nblocks[0] && !rc; ++i) {
+          const int idx[3] = {i + 1, j + 1, k + 1};
+          rc = fo_leaves(forest, nforest, &pos, 1, ndim, idx, leaves, &nl, nleafs);
+        }
+  } else {
+    /* build_block_info_morton (:183-226): the level-1 blocks in Morton order */
+    const long nb = (long)nblocks[0] * nblocks[1] * nblocks[2];
+    fo_mblock* mb = (fo_mblock*)malloc(sizeof(fo_mblock) * (size_t)nb);
+    long c = 0;
+    for (int k = 0; k < nblocks[2]; ++k)
+      for (int j = 0; j < nblocks[1]; ++j)
+        for (int i = 0; i < nblocks[0]; ++i) {
+          mb[c].code = fo_morton3((unsigned)i, (unsigned)j, (unsigned)k);
+          mb[c].i = i;
+          mb[c].j = j;
+          mb[c].k = k;
+          ++c;
+        }
+    qsort(mb, (size_t)nb, sizeof(fo_mblock), fo_mblock_cmp);
+    for (long b = 0; b < nb && !rc; ++b) {
+      const int idx[3] = {mb[b].i + 1, mb[b].j + 1, mb[b].k + 1};
+      rc = fo_leaves(forest, nforest, &pos, 1, ndim, idx, leaves, &nl, nleafs);
+    }
+    free(mb);
+  }
+  free(forest);
+  if (!rc && nl != nleafs) rc = FO_ETABLE; /* "block_info.size() ... does not match nleafs" */
+  const long npts = (long)nleafs * nglev1;
+  *ndim_out = ndim;
+  *npts_out = npts;
+  if (!rc && npts > cap) rc = FO_ECAP;
+  if (rc) {
+    free(leaves);
+    free(buf);
+    return rc;
+  }
+  /* fomo_from_amrvac (:228-299) */
+  const double R_spec = FO_BOLTZMANN / (0.5e0 * FO_MASS_PROTON);
+  const double V_unit = sqrt(R_spec * Teunit);
+  long boff = blockoff, p = 0;
+  for (long b = 0; b < nleafs; ++b) {
+    if (ghosts) boff += 8L * ndim;
+    const double* blk = (const double*)(buf + boff); /* nw variables, each nglev1 cells */
+    const int lev = leaves[b].level;
+    double bottomleft[3], lcs[3];
+    for (int j = 0; j < ndim; ++j) {
+      const double p2 = pow(2, lev - 1);
+      bottomleft[j] = xprobmin[j] + (leaves[b].idx[j] - 1) * cellsize[j] * nx[j] / p2;
+      lcs[j] = cellsize[j] / p2;
+    }
+    for (long k = 0; k < nglev1; ++k, ++p) {
+      const long lc[3] = {1 + k % nx[0], 1 + k / nx[0] % nx[0], 1 + k / nx[0] / nx[1]};
+      double cc[3] = {0, 0, 0};
+      for (int j = 0; j < ndim; ++j) {
+        cc[j] = bottomleft[j] + (lc[j] - .5) * lcs[j];
+        cc[j] *= L_unit;
+      }
+      double v[8];
+      for (int w = 0; w < 8 && w < nw; ++w) memcpy(&v[w], (const char*)blk + 8 * ((long)w * nglev1 + k), 8);
+      const double rho = v[0];
+      /* the kinetic and magnetic terms sum the first two components only (std::inner_product over [1, 3) and [5, 7)) */
+      const double kin = ((0. + v[1] * v[1]) + v[2] * v[2]) / rho / 2.;
+      const double mag = ((0. + v[5] * v[5]) + v[6] * v[6]) / 2.;
+      const double pr = (gamma - 1) * (v[4] - kin - mag);
+      x[p] = (float)cc[0];
+      y[p] = (float)cc[1];
+      z[p] = (float)cc[2];
+      n[p] = (float)(rho * n_unit);
+      T[p] = (float)(pr / rho * Teunit);
+      vx[p] = (float)(v[1] / rho * V_unit);
+      vy[p] = (float)(v[2] / rho * V_unit);
+      vz[p] = (float)(v[3] / rho * V_unit);
+    }
+    boff += 8L * nw * nglev1;
+  }
+  free(leaves);
+  free(buf);
+  return FO_OK;
+}

@@ -7,6 +7,7 @@
 // tests can generate golden vectors from the reference itself.
 //
 // This file is test infrastructure: nothing in the product library links it.
+#include <algorithm>
 #include <cstring>
 #include <iostream>
 #include <sstream>
@@ -16,6 +17,7 @@
 
 #include "FoMo.h"
 #include "FoMo-internal.h"  // has no include guard and needs FoMo.h first
+#include "FoMo-amrvac.h"    // the reference's AMRVAC reader (its example directory)
 
 namespace {
 
@@ -175,6 +177,36 @@ int ref_render_and_write(const char* method, long n, const float* x, const float
     FoMo::RenderCube r = obj.readrendering();
     r.setwriteoptions(std::bitset<FoMo::noptions>(static_cast<unsigned long>(options)));
     r.writegoftcube(out_path);
+    return 0;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return -1;
+  }
+}
+
+// The reference's AMRVAC snapshot reader (fomo-c/example/example_mpi_amrvac/
+// read_amrvac_files.cpp, compiled unmodified into this library): read a data
+// file into a FoMoObject and copy its DataCube out (coordinates, then n, T,
+// vx, vy, vz; z is left untouched for 2-D data).  -3 when cap is too small.
+int ref_amrvac_read(const char* datfile, const char* parfile, const char* amrvac_version, int gamma_eqparposition,
+                    double n_unit, double Teunit, double L_unit, long cap, int* ndim, long* npts, float* x,
+                    float* y, float* z, float* ne, float* T, float* vx, float* vy, float* vz) {
+  try {
+    QuietCout quiet;
+    FoMo::FoMoObject obj = read_amrvac_dat_file(datfile, parfile, amrvac_version, gamma_eqparposition, n_unit,
+                                                Teunit, L_unit);
+    FoMo::DataCube cube = obj.readdatacube();
+    FoMo::tgrid grid = cube.readgrid();
+    *ndim = (int)grid.size();
+    *npts = grid.empty() ? 0 : (long)grid[0].size();
+    if (*npts > cap) return -3;
+    float* c[3] = {x, y, z};
+    for (int d = 0; d < *ndim && d < 3; ++d) std::copy(grid[d].begin(), grid[d].end(), c[d]);
+    float* v[5] = {ne, T, vx, vy, vz};
+    for (int i = 0; i < 5; ++i) {
+      FoMo::tphysvar var = cube.readvar(i);
+      std::copy(var.begin(), var.end(), v[i]);
+    }
     return 0;
   } catch (const std::exception& e) {
     g_error = e.what();

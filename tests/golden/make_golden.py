@@ -15,8 +15,14 @@ synthetic cases and stores inputs and outputs as compressed .npz files:
     writer_*.txt/.dat the reference's own text and binary output files of three
                      small renders (spectroscopic, DN imaging, Thomson), with
                      their inputs in writers.npz
+    amrvac.npz       the points the reference's AMRVAC reader (fomo-c/example/
+                     example_mpi_amrvac/read_amrvac_files.cpp) reads from the
+                     synthetic data files of amrvac_files.py (3-D and 2-D AMR,
+                     version 4 and pre-2017 formats, both leaf orders), with the
+                     files' SHA-256 (the writer is deterministic)
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [amrvac]
+(``amrvac`` regenerates amrvac.npz only.)
 The fixtures are committed; the GPU machine has no reference tree and only reads them.
 """
 
@@ -156,5 +162,29 @@ def main():
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
+def make_amrvac():
+    import hashlib
+
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import amrvac_files as A
+
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        for name in A.CASES:
+            dat, par, kw = A.write_case(name, td)
+            nd, arrs = oracle.ref_amrvac_read(dat, par, kw["amrvac_version"], kw["gamma_eqparposition"], kw["n_unit"],
+                                              kw["Teunit"], kw["L_unit"])
+            out[name + "_sha256"] = np.array(hashlib.sha256(open(dat, "rb").read()).hexdigest())
+            if par:
+                out[name + "_par_sha256"] = np.array(hashlib.sha256(open(par, "rb").read()).hexdigest())
+            out[name + "_ndim"] = np.array(nd)
+            for key, a in zip(("x", "y", "z", "n", "T", "vx", "vy", "vz"), arrs):
+                out[f"{name}_{key}"] = a
+    np.savez_compressed(os.path.join(ROOT, "tests", "golden", "amrvac.npz"), **out)
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1 and sys.argv[1] == "amrvac":
+        make_amrvac()
+        sys.exit(0)
     main()
