@@ -1187,10 +1187,29 @@ __device__ __forceinline__ void lane_scan(const SnapDev& S, const BoxQ& q, int p
     scan_point<EXACT>(__ldg(S.pts + FOMO_IDX(p, S.n, kSitePts)), p, q, band, best, second, bpos, borig, bD);
 }
 
+// Narrow the cell range [lo, hi] of one axis to the cells whose gap from t can
+// be within sqrt(rem) (none when rem < 0).  A superset: the reach carries the
+// same relative and cell-margin slack as the x-range clip of a row.
+__device__ __forceinline__ void clip_reach(float rem, float t, float o, float inv_h, float h, int dim, int& lo,
+                                           int& hi) {
+  if (rem < 0.0f) {
+    hi = lo - 1;
+    return;
+  }
+  const float r = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
+  lo = max(lo, cell_coord(t - r, o, inv_h, dim));
+  hi = min(hi, cell_coord(t + r, o, inv_h, dim));
+}
+
 // One lane's walk over the rings of cells around the target's cell c (clamped
 // into the grid), nearest first.  A ring, a row or a cell is skipped when its
 // lower bound from the target exceeds the bound (the best squared distance so
 // far, or `band` in the EXACT pass); every loop is bounded by the box's cells.
+// Within a ring only the rows that can pass are enumerated: the z planes
+// within the bound, in each the y range within it, and of the rows inside the
+// ring's y-z square (which hold just the ring's two x-end cells) those whose
+// end cells can pass.  The skipped rows would all fail the per-row test, so
+// the rows scanned, and the result, are those of a walk over every row.
 template <bool EXACT, bool BUDGET>
 __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, const int (&b0)[3], const int (&b1)[3],
                                            const int (&c)[3], const float (&gc)[3], float band, float& best,
@@ -1219,20 +1238,42 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
     const bool has_l = xl >= b0[0], has_r = s > 0 && xr <= b1[0];
     const float gxl = has_l ? axis_gap(xl, q.tx, g.ox, h) : 0.0f;
     const float gxr = has_r ? axis_gap(xr, q.tx, g.ox, h) : 0.0f;
-    const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
-    const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
+    // the smaller squared x gap of the ring's end cells (rows inside its y-z square); -1: no end cell
+    const float gxe2 = (has_l || has_r) ? fminf(has_l ? gxl * gxl : FLT_MAX, has_r ? gxr * gxr : FLT_MAX) : -1.0f;
+    // rings of up to 3 x 3 rows are walked whole: their clipping would cost more than the rows it saves
+    const bool clip = s >= 2;
+    int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
+    if (clip) {
+      const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
+      if (bound < FLT_MAX) clip_reach(bound - gc[0], q.tz, g.oz, g.inv_h, h, g.dz, z0, z1);
+    }
     for (int kz = z0; kz <= z1; ++kz) {
       const float gz = axis_gap(kz, q.tz, g.oz, h);
       const float gz2 = gz * gz;
       const bool zshell = kz == c[2] - s || kz == c[2] + s;
-      for (int jy = y0; jy <= y1; ++jy) {
+      const float bz = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
+      int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
+      // interior rows [ilo, ihi]: strictly inside the ring's y range, end cells within the bound
+      int ilo = c[1] - s + 1, ihi = c[1] + s - 1;
+      if (!zshell && gxe2 < 0.0f) ihi = ilo - 1;
+      if (clip && bz < FLT_MAX) {
+        clip_reach(bz - gc[0] - gz2, q.ty, g.oy, g.inv_h, h, g.dy, y0, y1);
+        if (!zshell && gxe2 >= 0.0f) clip_reach(bz - gxe2 - gz2, q.ty, g.oy, g.inv_h, h, g.dy, ilo, ihi);
+      }
+      for (int jy = y0; jy <= y1;) {
+        const bool face = zshell || jy == c[1] - s || jy == c[1] + s;
+        if (!face && (jy < ilo || jy > ihi)) {
+          jy = (jy < ilo && ilo <= ihi) ? ilo : c[1] + s;  // the next interior row that can pass, or the far face
+          continue;
+        }
         if (BUDGET && budget < 0) return;  // out of budget: a warp searches this sample
         const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
         const float gy = axis_gap(jy, q.ty, g.oy, h);
         const float gyz = fmaf(gy, gy, gz2);
-        if (gyz + gc[0] > bound) continue;
         const int rowbase = (kz * g.dy + jy) * g.dx;
-        if (zshell || jy == c[1] - s || jy == c[1] + s) {
+        if (gyz + gc[0] > bound) {
+          // this row cannot pass
+        } else if (face) {
           // a row on the ring's y/z faces: its x-range within the bound
           int x0 = max(xl, b0[0]), x1 = min(xr, b1[0]);
           if (bound < FLT_MAX) {
@@ -1256,6 +1297,7 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
                                      __ldg(S.cell_start + FOMO_IDX(rowbase + xr + 1, cell_entries(g), kSiteCellStart)),
                                      band, best, second, bpos, borig, bD, budget);
         }
+        ++jy;
       }
     }
   }
@@ -1362,9 +1404,13 @@ __device__ __forceinline__ void warp_rings(const SnapDev& S, const BoxQ& q, cons
     const bool has_l = xl >= b0[0], has_r = s > 0 && xr <= b1[0];
     const float gxl = has_l ? axis_gap(xl, q.tx, g.ox, h) : 0.0f;
     const float gxr = has_r ? axis_gap(xr, q.tx, g.ox, h) : 0.0f;
-    const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
-    const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
-    const int nyr = y1 - y0 + 1, nrows = nyr * (z1 - z0 + 1);
+    int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
+    int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
+    if (bound < FLT_MAX) {  // the ring's y-z square narrowed to the rows within the bound
+      clip_reach(bound - gc[0], q.tz, g.oz, g.inv_h, h, g.dz, z0, z1);
+      clip_reach(bound - gc[0], q.ty, g.oy, g.inv_h, h, g.dy, y0, y1);
+    }
+    const int nyr = y1 - y0 + 1, nrows = (nyr > 0 && z1 >= z0) ? nyr * (z1 - z0 + 1) : 0;
     for (int rb = 0; rb < nrows; rb += 32) {
       // this lane's row of the ring: up to two point ranges
       const int rr = rb + lane;

@@ -1097,6 +1097,10 @@ int fomo_ctx_create(int device, size_t hbm_budget_bytes, fomo_ctx** out) {
       ctx->print_stats = true;
     }
   }
+  if (const char* co = std::getenv("FOMO_CELL_OCCUPANCY")) {
+    const double v = std::atof(co);  // target points per grid cell of the snapshots built afterwards
+    if (v >= 0.25 && v <= 64.0) ctx->cell_occupancy = v;
+  }
   if (const char* fa = std::getenv("FOMO_INJECT_ALLOC_FAILURE")) ctx->fail_alloc_at = std::atol(fa);
   const char* tm = std::getenv("FOMO_TIME_MARCH");
   ctx->time_march = !(tm && tm[0] == '0');

@@ -26,6 +26,9 @@ pytestmark = pytest.mark.gpu
 N_POINTS = 8 * 1024 * 1024
 CHANNELS = (94, 131, 171, 193, 211, 335)
 TOL = 1e-4
+DN6 = "8M-point flux rope, 6 DN channels, 1024x1024 px, 1024 samples (sampled rows)"
+THOMSON = "8M-point flux rope at 1.5 Rsun, Thomson pB, b = 0.3, 1024x1024 px (sampled rows)"
+WIDE = "512K-point flux rope, 64x64 px, 16 bins, 256 samples, wide boxes (full cubes)"
 
 
 @pytest.fixture(scope="module")
@@ -53,7 +56,7 @@ def test_six_dn_channels_full_size_sampled_rows(ctx, rope):
             oc, _, ov = oracle.nn_render(rope, eps, w, tabs[k].lambda0, l, b, 1024, 1024, 1024, 1, 1e5, is_dn=True,
                                          rows=(r0, r0 + 1))
             assert infos[k].maxdistance == ov[oracle.V_MAXDIST] and infos[k].apix == ov[oracle.V_APIX]
-            assert G.norm_max_err(cubes[k][r0:r0 + 1].ravel(), oc.ravel()) <= TOL
+            assert G.record(DN6, cubes[k][r0:r0 + 1].ravel(), oc.ravel()) <= TOL
     # neighbour indices at 256 x 256 (1024 samples per ray), sampled rows
     q = ctx.request(sid, tids[2], fg.METHOD_NN, 256, 256, 1024, 1, l, b, 1e5)
     cube, idx, info = ctx.render(q, want_idx=True)
@@ -61,6 +64,7 @@ def test_six_dn_channels_full_size_sampled_rows(ctx, rope):
     for r0 in (40, 128, 230):
         oc, oi, _ = oracle.nn_render(rope, eps, w, tabs[2].lambda0, l, b, 256, 256, 1024, 1, 1e5, is_dn=True,
                                      rows=(r0, r0 + 1), want_idx=True)
+        G.record_idx(DN6, idx[r0:r0 + 1], oi)
         np.testing.assert_array_equal(idx[r0:r0 + 1], oi)
     ctx.drop_snapshot(sid)
 
@@ -75,12 +79,13 @@ def test_thomson_off_equator_full_size_sampled_rows(ctx):
     for r0 in (600,):  # the oracle's far searches take seconds per row
         oc, _, ov = oracle.thomson_render(ts, tot, pol, l, b, 1024, 1024, 1024, rows=(r0, r0 + 1))
         assert info.maxdistance == ov[oracle.V_MAXDIST]
-        assert G.norm_max_err(cube[r0:r0 + 1].ravel(), oc.ravel()) <= TOL
+        assert G.record(THOMSON, cube[r0:r0 + 1].ravel(), oc.ravel()) <= TOL
     q = ctx.request(sid, 0, fg.METHOD_THOMSON, 256, 256, 1024, 1, l, b, 1e5)
     cube, idx, info = ctx.render(q, want_idx=True)
     assert (idx >= 0).mean() > 0.9  # the wide boxes give nearly every sample a neighbour
     for r0 in (20, 131):
         _, oi, _ = oracle.thomson_render(ts, tot, pol, l, b, 256, 256, 1024, rows=(r0, r0 + 1), want_idx=True)
+        G.record_idx(THOMSON, idx[r0:r0 + 1], oi)
         np.testing.assert_array_equal(idx[r0:r0 + 1], oi)
     ctx.drop_snapshot(sid)
 
@@ -98,7 +103,8 @@ def test_wide_boxes_dense_cells_full_cube(ctx):
     for (l, b) in ((0.5, 0.2), (1.2, -0.3)):
         cube, idx, _ = ctx.render(ctx.request(sid, tid, fg.METHOD_NN, 64, 64, 256, 16, l, b, width), want_idx=True)
         oc, oi, _ = oracle.nn_render(s, eps, w, t.lambda0, l, b, 64, 64, 256, 16, width, want_idx=True)
+        G.record_idx(WIDE, idx, oi)
         np.testing.assert_array_equal(idx, oi)
-        assert G.norm_max_err(cube.ravel(), oc.ravel()) <= TOL
+        assert G.record(WIDE, cube.ravel(), oc.ravel()) <= TOL
     ctx.drop_snapshot(sid)
 

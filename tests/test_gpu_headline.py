@@ -29,6 +29,8 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-4  # max|g - o| / max|o| against the FP64 oracle
 ROWS = ((1, 3), (127, 129), (253, 255))  # image rows compared: both edges and the middle
+BATCHED = "batched 2M-point loop, 64 views x 4 lines, 256x256 px, 64 bins, 512 samples (sampled rows)"
+PLAIN = "plain 2M-point loop, 512x512 px, 128 bins, 512 samples, l = 0/30/60 (sampled rows)"
 
 
 @pytest.fixture(scope="module")
@@ -81,11 +83,12 @@ def test_batched_workload_graph_replays_match_oracle(workload):
                                                       bench.NX, bench.NY, bench.NZ, bench.NL, bench.WIDTH,
                                                       rows=(r0, r1), want_idx=(li == 0))
                         if li == 0:
+                            G.record_idx(BATCHED, idx[r0:r1], oi)
                             np.testing.assert_array_equal(idx[r0:r1], oi)
                         assert info.maxdistance == ov[oracle.V_MAXDIST]
                         assert info.pathlength == ov[oracle.V_PATHLENGTH]
                         if np.abs(oc).max() > 0:
-                            err = G.norm_max_err(got[r0:r1].ravel(), oc.ravel())
+                            err = G.record(BATCHED, got[r0:r1].ravel(), oc.ravel())
                             assert err <= TOL, (v, li, r0, err)
                 assert (idx >= 0).mean() > 0.3  # the views do see the loop
         ctx.drop_snapshot(sid)
@@ -114,8 +117,9 @@ def test_plain_config_views_sampled_rows(plain, l_deg):
     for r0 in (3, 255, 509):
         oc, oi, ov = oracle.nn_render(s, eps, w, t.lambda0, l, 0.0, 512, 512, 512, 128, width, rows=(r0, r0 + 2),
                                       want_idx=True)
+        G.record_idx(PLAIN, idx[r0:r0 + 2], oi)
         np.testing.assert_array_equal(idx[r0:r0 + 2], oi)
         assert info.maxdistance == ov[oracle.V_MAXDIST]
         if np.abs(oc).max() > 0:
-            assert G.norm_max_err(cube[r0:r0 + 2].ravel(), oc.ravel()) <= TOL
+            assert G.record(PLAIN, cube[r0:r0 + 2].ravel(), oc.ravel()) <= TOL
     assert (idx >= 0).mean() > 0.5

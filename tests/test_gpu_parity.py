@@ -54,9 +54,10 @@ def test_spectroscopic_golden(ctx, name):
         cube, idx, info = ctx.render(req, want_idx=True)
         ocube, oidx, oview = oracle.nn_render(s, d["eps"], d["fwhm"], t.lambda0, l, b, nx, ny, nz, L, width,
                                               want_idx=True)
+        G.record_idx("golden " + name, idx, oidx)
         np.testing.assert_array_equal(idx, oidx)          # neighbours bit-exact
         _check_view(info, oview)
-        assert G.norm_max_err(cube.ravel(), ocube.ravel()) <= TOL      # vs FP64 oracle
+        assert G.record("golden " + name, cube.ravel(), ocube.ravel()) <= TOL      # vs FP64 oracle
         assert G.norm_max_err(cube.ravel(), d["cube"][v]) <= TOL       # vs the reference's own cube
         assert G.l2_rel_err(cube.ravel(), ocube.ravel()) <= TOL
     ctx.drop_snapshot(sid)
@@ -95,10 +96,11 @@ def test_imaging_dn_golden(ctx):
         cube, idx, info = ctx.render(req, want_idx=True)
         ocube, oidx, oview = oracle.nn_render(s, d["eps"], d["fwhm"], t.lambda0, l, b, nx, ny, nz, 1,
                                               d["meta"][v][4], is_dn=True, want_idx=True)
+        G.record_idx("golden nn_imaging.npz", idx, oidx)
         np.testing.assert_array_equal(idx, oidx)
         assert info.is_dn == 1 and info.observation_type == fg.OBS_IMAGING
         assert info.apix == oview[oracle.V_APIX]
-        assert G.norm_max_err(cube.ravel(), ocube.ravel()) <= TOL
+        assert G.record("golden nn_imaging.npz", cube.ravel(), ocube.ravel()) <= TOL
         assert G.norm_max_err(cube.ravel(), d["cube"][v]) <= TOL
         gx, gy, _ = fg.render_grid(nx, ny, 1, info, True)
         np.testing.assert_array_equal(gx, d["gx"][v])
@@ -115,9 +117,10 @@ def test_thomson_golden(ctx):
         req = ctx.request(sid, 0, fg.METHOD_THOMSON, nx, ny, nz, 1, l, b, 1e5)
         cube, idx, info = ctx.render(req, want_idx=True)
         ocube, oidx, oview = oracle.thomson_render(s, d["tot"], d["pol"], l, b, nx, ny, nz, want_idx=True)
+        G.record_idx("golden thomson.npz", idx, oidx)
         np.testing.assert_array_equal(idx, oidx)
         _check_view(info, oview)
-        assert G.norm_max_err(cube.ravel(), ocube.ravel()) <= TOL
+        assert G.record("golden thomson.npz", cube.ravel(), ocube.ravel()) <= TOL
         assert G.norm_max_err(cube.ravel(), d["cube"][v]) <= TOL
     ctx.drop_snapshot(sid)
 
@@ -142,6 +145,9 @@ def test_edges_golden(ctx):
     ctx.drop_snapshot(sid)
 
 
+LOOP64 = "262K-point loop, 128x128 px, 64 bins, 256 samples, 3 views (full cubes)"
+
+
 @pytest.mark.parametrize("l,b", [(0.0, 0.0), (0.5236, 0.0), (0.4, -0.3)])
 def test_loop_64cubed_reference_scale(ctx, l, b):
     """The CPU-scale loop (64^3 points, 128x128 pixels, 64 bins, 256 samples) with b = 0 and b != 0."""
@@ -154,9 +160,10 @@ def test_loop_64cubed_reference_scale(ctx, l, b):
     req = ctx.request(sid, tid, fg.METHOD_NN, 128, 128, 256, 64, l, b, width)
     cube, idx, info = ctx.render(req, want_idx=True)
     ocube, oidx, oview = oracle.nn_render(s, eps, w, t.lambda0, l, b, 128, 128, 256, 64, width, want_idx=True)
+    G.record_idx(LOOP64, idx, oidx)
     np.testing.assert_array_equal(idx, oidx)
     _check_view(info, oview)
-    assert G.norm_max_err(cube.ravel(), ocube.ravel()) <= TOL
+    assert G.record(LOOP64, cube.ravel(), ocube.ravel()) <= TOL
     ctx.drop_snapshot(sid)
 
 
