@@ -30,9 +30,10 @@ OBS_SPECTROSCOPIC = 1
 OBS_IMAGING = 2
 SPEED_OF_LIGHT = 2.99792458e8
 # FOMO_KERNEL_* and FOMO_COUNTER_* of include/fomo_gpu.h, in order
-KERNELS = ("search", "split", "deferred", "hard", "emission", "fused")
+KERNELS = ("search", "split", "deferred", "hard", "emission", "fused", "far")
 COUNTERS = ("segments", "candidates", "rows", "points_loaded", "not_gathered", "fallbacks", "samples", "scanned",
-            "ties", "fb_nocand", "fb_far", "fb_ambiguous", "deferred", "deferred_recs", "hard", "runs", "ex2")
+            "ties", "fb_nocand", "fb_far", "fb_ambiguous", "deferred", "deferred_recs", "hard", "runs", "ex2",
+            "far_groups", "far")
 
 
 class FomoError(RuntimeError):

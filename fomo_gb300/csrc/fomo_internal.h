@@ -80,15 +80,18 @@ struct LineDesc {
 // deferred-record queue head, the number of overflow records written from the
 // back (segments whose capsule held too many points), their queue head, the
 // number of hard samples queued for a warp each, their queue head, the ray
-// queue head of the emission pass of the two-pass spectral march.
+// queue head of the emission pass of the two-pass spectral march, the number
+// of records flagged for the far pass and its queue head.
 enum MarchCounter {
   kCtrRays = 0, kCtrDeferred, kCtrDeferredHead, kCtrOverflow, kCtrOverflowHead, kCtrHard, kCtrHardHead, kCtrShade,
+  kCtrFar, kCtrFarHead,
   kCtrCount
 };
 
 // One segment whose samples the march's first search pass could not resolve:
-// x = work item of the ray, y = first LOS sample of the segment, z/w = masks
-// of the unresolved samples y + lane and y + 32 + lane.
+// x = work item of the ray, y = first LOS sample of the segment (bits 0-29;
+// bits 30 and 31 flag the halves the far pass may take), z/w = masks of the
+// unresolved samples y + lane and y + 32 + lane.
 using DeferredRec = uint4;
 
 struct MarchArgs {
@@ -103,6 +106,7 @@ struct MarchArgs {
   unsigned long long* counter;   // kCtrCount work counters, zeroed before the launch
   DeferredRec* deferred;         // one record per segment at most: capacity deferred_cap
   int64_t deferred_cap;
+  int32_t* far_list;             // slots of the records flagged for the far pass (capacity deferred_cap), or null
   uint2* hard;                   // deferred samples (work item, sample) for a whole warp each, or null
   int64_t hard_cap;              // its capacity (0: every deferred sample is searched by one lane)
   int32_t* const* nn_idx;        // per view (nullable array / entries), [ray][nz] original index
@@ -133,12 +137,14 @@ enum MarchStat {
   kStatHard,           // deferred samples whose one-lane search ran out of budget (searched by a warp)
   kStatRuns,           // runs of equal neighbours binned by the spectral emission pass (with a neighbour)
   kStatEx2,            // ex2 evaluations of the spectral emission pass (32 per run, line and 32-bin window)
+  kStatFarGroups,      // record halves searched together by the far pass
+  kStatFar,            // deferred samples the far pass resolved
   kStatCount
 };
 
 // Kernels of one march, for optional per-kernel timing (direct launches
 // only): events recorded on the stream after each kernel, tagged with its kind.
-enum MarchKernel : int { kKSearch = 0, kKSplit, kKDeferred, kKHard, kKEmission, kKFused, kKCount };
+enum MarchKernel : int { kKSearch = 0, kKSplit, kKDeferred, kKHard, kKEmission, kKFused, kKFar, kKCount };
 struct MarchTimer {
   cudaEvent_t* ev = nullptr;  // pool of `cap` events
   int* kind = nullptr;        // kind of the kernel that ends at ev[i]; -1 marks a start

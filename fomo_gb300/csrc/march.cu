@@ -4,9 +4,11 @@
 //
 // Kernels, in stream order: march_search (stores each sample's neighbour in a
 // position buffer), march_split (segments whose capsule overflowed),
-// march_deferred (samples the search could not resolve, one lane each),
-// march_hard (deferred samples over a lane's budget, one warp each) -- the
-// last three store the neighbours they find in the same buffer -- and then the
+// march_far (deferred samples far off the points, searched together),
+// march_deferred (the other samples the search could not resolve, one lane
+// each), march_hard (deferred samples over
+// a lane's budget, one warp each) -- the last four store the neighbours they
+// find in the same buffer -- and then the
 // emission pass, march_spectral<.., shade> or march_imaging<.., shade>, which
 // bins every ray from the buffer.  The no-allocation path has no buffer: its
 // first pass (march_spectral / march_imaging, fused) searches and bins, and
@@ -87,6 +89,18 @@ constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
 constexpr int kSegCap = 176;          // candidates per segment (sized so that 7 search CTAs fit an SM)
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule beyond which it is deferred
 constexpr float kRScaleDefault = 0.9f;  // gather radius in local point spacings (MarchArgs::rscale when set)
+// Far pass (march_far): samples two cells or more off the points' bounding box,
+// kFarMin or more of them in a half record, searched together by a warp.
+constexpr int kFarMin = 8;          // far samples a half needs (fewer: the lane walks of march_deferred)
+constexpr float kFarOut2 = 4.0f;    // squared distance, in cells, off the points' bounding box of a far sample
+constexpr float kFarBox = 8.0f;     // box half-width, in cells, of the views the far pass takes (narrower: lane walks)
+constexpr int kFarIters = 4;        // gathers per half
+constexpr int kFarMaxPts = 1024;    // points of a gather beyond which the half is left to march_deferred
+// A deferred record is (work item, first sample of its 64-sample segment with
+// two flags above it, samples 0-31 of the segment as a bit mask, samples 32-63).
+constexpr unsigned kRecS0 = (1u << 30) - 1u;  // the first sample
+constexpr unsigned kRecFar0 = 1u << 30;       // samples 0-31 hold kFarMin far samples or more
+constexpr unsigned kRecFar1 = 1u << 31;       // samples 32-63 do
 
 
 struct __align__(16) SegSmem {
@@ -845,8 +859,35 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
     const bool over = !gathered && nseg > 16;
     const unsigned long long k = atomicAdd(a.counter + (over ? kCtrOverflow : kCtrDeferred), 1ull);
     const int64_t slot = over ? a.deferred_cap - 1 - (int64_t)k : (int64_t)k;
-    if (slot >= 0 && slot < a.deferred_cap)  // always: the capacity is one record per segment
-      a.deferred[FOMO_IDX(slot, a.deferred_cap, kSiteDeferred)] = make_uint4(r.item, (unsigned)s0, f0, f1);
+    // the halves the far pass may take, in views whose boxes reach kFarBox
+    // cells or more from their target: kFarMin or more deferred samples, the
+    // whole half two cells or more off the points' bounding box (the box of
+    // the half's stretch of the segment against the points' box)
+    unsigned flags = 0u;
+    bool listed = false;
+    if (a.far_list && r.mdf >= kFarBox * g.h) {
+      const float inv = nseg > 1 ? 1.0f / (float)(nseg - 1) : 0.0f;
+      const float off2 = kFarOut2 * g.h * g.h;
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        if (__popc(hh ? f1 : f0) < kFarMin) continue;
+        const float t0 = (float)(32 * hh) * inv, t1 = (float)min(32 * hh + 31, nseg - 1) * inv;
+        const float xa = fmaf(t0, sdx, ax), xb = fmaf(t1, sdx, ax), ya = fmaf(t0, sdy, ay), yb = fmaf(t1, sdy, ay),
+                    za = fmaf(t0, sdz, az), zb = fmaf(t1, sdz, az);
+        const float ex = fmaxf(fmaxf(g.minx - fmaxf(xa, xb), fminf(xa, xb) - g.maxx), 0.0f);
+        const float ey = fmaxf(fmaxf(g.miny - fmaxf(ya, yb), fminf(ya, yb) - g.maxy), 0.0f);
+        const float ez = fmaxf(fmaxf(g.minz - fmaxf(za, zb), fminf(za, zb) - g.maxz), 0.0f);
+        if (fmaf(ez, ez, fmaf(ey, ey, ex * ex)) >= off2) flags |= hh ? kRecFar1 : kRecFar0;
+      }
+      listed = flags != 0u;
+    }
+    if (slot >= 0 && slot < a.deferred_cap) {  // always: the capacity is one record per segment
+      a.deferred[FOMO_IDX(slot, a.deferred_cap, kSiteDeferred)] = make_uint4(r.item, (unsigned)s0 | flags, f0, f1);
+      if (listed) {
+        const unsigned long long f = atomicAdd(a.counter + kCtrFar, 1ull);
+        if ((int64_t)f < a.deferred_cap) a.far_list[FOMO_IDX(f, a.deferred_cap, kSiteDeferred)] = (int32_t)slot;
+      }
+    }
   }
   if (stats) {
     const unsigned sc = __reduce_add_sync(kFull, (unsigned)st_scanned);
@@ -1205,11 +1246,6 @@ __device__ __forceinline__ void clip_reach(float rem, float t, float o, float in
 // into the grid), nearest first.  A ring, a row or a cell is skipped when its
 // lower bound from the target exceeds the bound (the best squared distance so
 // far, or `band` in the EXACT pass); every loop is bounded by the box's cells.
-// Within a ring only the rows that can pass are enumerated: the z planes
-// within the bound, in each the y range within it, and of the rows inside the
-// ring's y-z square (which hold just the ring's two x-end cells) those whose
-// end cells can pass.  The skipped rows would all fail the per-row test, so
-// the rows scanned, and the result, are those of a walk over every row.
 template <bool EXACT, bool BUDGET>
 __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, const int (&b0)[3], const int (&b1)[3],
                                            const int (&c)[3], const float (&gc)[3], float band, float& best,
@@ -1238,42 +1274,20 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
     const bool has_l = xl >= b0[0], has_r = s > 0 && xr <= b1[0];
     const float gxl = has_l ? axis_gap(xl, q.tx, g.ox, h) : 0.0f;
     const float gxr = has_r ? axis_gap(xr, q.tx, g.ox, h) : 0.0f;
-    // the smaller squared x gap of the ring's end cells (rows inside its y-z square); -1: no end cell
-    const float gxe2 = (has_l || has_r) ? fminf(has_l ? gxl * gxl : FLT_MAX, has_r ? gxr * gxr : FLT_MAX) : -1.0f;
-    // rings of up to 3 x 3 rows are walked whole: their clipping would cost more than the rows it saves
-    const bool clip = s >= 2;
-    int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
-    if (clip) {
-      const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
-      if (bound < FLT_MAX) clip_reach(bound - gc[0], q.tz, g.oz, g.inv_h, h, g.dz, z0, z1);
-    }
+    const int z0 = max(c[2] - s, b0[2]), z1 = min(c[2] + s, b1[2]);
+    const int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
     for (int kz = z0; kz <= z1; ++kz) {
       const float gz = axis_gap(kz, q.tz, g.oz, h);
       const float gz2 = gz * gz;
       const bool zshell = kz == c[2] - s || kz == c[2] + s;
-      const float bz = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
-      int y0 = max(c[1] - s, b0[1]), y1 = min(c[1] + s, b1[1]);
-      // interior rows [ilo, ihi]: strictly inside the ring's y range, end cells within the bound
-      int ilo = c[1] - s + 1, ihi = c[1] + s - 1;
-      if (!zshell && gxe2 < 0.0f) ihi = ilo - 1;
-      if (clip && bz < FLT_MAX) {
-        clip_reach(bz - gc[0] - gz2, q.ty, g.oy, g.inv_h, h, g.dy, y0, y1);
-        if (!zshell && gxe2 >= 0.0f) clip_reach(bz - gxe2 - gz2, q.ty, g.oy, g.inv_h, h, g.dy, ilo, ihi);
-      }
-      for (int jy = y0; jy <= y1;) {
-        const bool face = zshell || jy == c[1] - s || jy == c[1] + s;
-        if (!face && (jy < ilo || jy > ihi)) {
-          jy = (jy < ilo && ilo <= ihi) ? ilo : c[1] + s;  // the next interior row that can pass, or the far face
-          continue;
-        }
+      for (int jy = y0; jy <= y1; ++jy) {
         if (BUDGET && budget < 0) return;  // out of budget: a warp searches this sample
         const float bound = EXACT ? band * (1.0f + kRelPrune) : best * (1.0f + kRelPrune);
         const float gy = axis_gap(jy, q.ty, g.oy, h);
         const float gyz = fmaf(gy, gy, gz2);
+        if (gyz + gc[0] > bound) continue;
         const int rowbase = (kz * g.dy + jy) * g.dx;
-        if (gyz + gc[0] > bound) {
-          // this row cannot pass
-        } else if (face) {
+        if (zshell || jy == c[1] - s || jy == c[1] + s) {
           // a row on the ring's y/z faces: its x-range within the bound
           int x0 = max(xl, b0[0]), x1 = min(xr, b1[0]);
           if (bound < FLT_MAX) {
@@ -1297,7 +1311,6 @@ __device__ __forceinline__ void lane_rings(const SnapDev& S, const BoxQ& q, cons
                                      __ldg(S.cell_start + FOMO_IDX(rowbase + xr + 1, cell_entries(g), kSiteCellStart)),
                                      band, best, second, bpos, borig, bD, budget);
         }
-        ++jy;
       }
     }
   }
@@ -1656,7 +1669,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
     RayCtx r;
     if (!ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, r)) continue;  // records come from real rays only
     const ViewDesc* V = a.views + r.v;
-    const int nz = V->nz, s0 = (int)rec.y;
+    const int nz = V->nz, s0 = (int)(rec.y & kRecS0);
     PartIn in;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
@@ -1706,6 +1719,263 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
   }
 }
 
+// ---------------------------------------------------------------------------
+// Far samples: the deferred samples of one half of a record (up to 32
+// consecutive LOS samples of one ray, lane = sample) that lie two cells or
+// more outside the points' bounding box, searched together; the search pass
+// flags the halves that hold kFarMin of them or more.  Such samples lie away
+// from the points (wide boxes off the cloud, as Thomson's far from the
+// equator): each one's own ring walk would scan every cell of the lens where
+// the ball of its neighbour's distance cuts into the cloud, and consecutive
+// samples scan almost the same lens.  Here each pending sample gets a ball --
+// at first its distance to the points' bounding box plus two cells -- and
+// each lane marks, in shared memory, the x range its ball covers in every row
+// of cells it reaches; the warp then gathers those rows (the union of the
+// balls), testing each gathered point against every sample's box as the
+// one-lane search does.  A sample whose best point lies
+// inside its own ball (gathered whole), without a near-tie, has its neighbour;
+// the others take a ball through their best point, or a margin twice as wide
+// when they found none, and the warp gathers again.  Samples still open after
+// kFarIters gathers, near-ties and gathers beyond the row or point bounds go
+// on to march_deferred as before.
+// ---------------------------------------------------------------------------
+constexpr int kMinCtasFar = 6;
+
+constexpr int kFarRowCap = 256;  // rows of a gather's bounding rectangle (beyond: the half is left)
+struct __align__(16) FarSmem {
+  float4 pt[32];           // a round of gathered points
+  int pp[32];              // their sorted positions
+  int xlo[kFarRowCap];     // per row of the rectangle: the union of the balls' chords, as ordered ints
+  int xhi[kFarRowCap];
+};
+
+// float -> int with the same order (atomicMin / atomicMax on floats)
+__device__ __forceinline__ int ford(float f) {
+  const int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fdeord(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+// Warp-collective search of the lanes' samples (act: this lane holds one, box
+// q).  Returns the lanes whose neighbour was found: pos / orig set, -1 when
+// the box holds no point.
+__device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bool act, FarSmem& fs, int& pos,
+                                             int& orig) {
+  const GridParams& g = S.g;
+  const float h = g.h;
+  const int lane = threadIdx.x & 31;
+  pos = -1;
+  orig = -1;
+  int b0[3], b1[3], c[3];
+  float gc[3];
+  const bool in_grid = act && box_cells(g, q, b0, b1, c, gc);
+  unsigned solved = __ballot_sync(kFull, act && !in_grid);  // the box misses the points' bounding box
+  // squared distance from the target to the points' bounding box: a lower
+  // bound of its neighbour's
+  const float dxg = fmaxf(fmaxf(g.minx - q.tx, q.tx - g.maxx), 0.0f);
+  const float dyg = fmaxf(fmaxf(g.miny - q.ty, q.ty - g.maxy), 0.0f);
+  const float dzg = fmaxf(fmaxf(g.minz - q.tz, q.tz - g.maxz), 0.0f);
+  const float L2 = fmaf(dzg, dzg, fmaf(dyg, dyg, dxg * dxg));
+  float margin2 = 4.0f * h * h;  // the ball's margin beyond that bound, squared: two cells at first
+  float r2 = L2 + margin2;
+  // far samples only (two cells or more off the points): near and inside the
+  // cloud the balls' union holds too many points for every lane to test
+  unsigned pend = __ballot_sync(kFull, in_grid && L2 >= kFarOut2 * h * h);
+  if (__popc(pend) < kFarMin) pend = 0;
+  for (int it = 0; it < kFarIters && pend; ++it) {
+    const bool mine = (pend >> lane) & 1u;
+    float best = FLT_MAX, second = FLT_MAX;
+    int bpos = -1, borig = -1;
+    double bD = DBL_MAX;
+    // the rows this lane's ball reaches: the (y, z) disc where it meets the
+    // grid's x range, within the box
+    float ylo = FLT_MAX, yhi = -FLT_MAX, zlo = FLT_MAX, zhi = -FLT_MAX;
+    if (mine) {
+      const float rho2 = r2 - dxg * dxg;
+      if (rho2 >= 0.0f) {
+        const float rho = (rho2 > 0.0f ? rho2 * rsqrtf(rho2) * 1.0001f : 0.0f) + kCellMargin * h;
+        ylo = fmaxf(q.ty - rho, q.loy);
+        yhi = fminf(q.ty + rho, q.hiy);
+        zlo = fmaxf(q.tz - rho, q.loz);
+        zhi = fminf(q.tz + rho, q.hiz);
+      }
+    }
+    ylo = warp_min(ylo);
+    yhi = warp_max(yhi);
+    zlo = warp_min(zlo);
+    zhi = warp_max(zhi);
+    bool overflow = false;
+    int j0 = 0, k0 = 0, nyr = 0, nrows = 0;
+    if (ylo <= yhi && zlo <= zhi) {
+      j0 = cell_coord(ylo, g.oy, g.inv_h, g.dy);
+      const int j1 = cell_coord(yhi, g.oy, g.inv_h, g.dy);
+      k0 = cell_coord(zlo, g.oz, g.inv_h, g.dz);
+      const int k1 = cell_coord(zhi, g.oz, g.inv_h, g.dz);
+      nyr = j1 - j0 + 1;
+      nrows = nyr * (k1 - k0 + 1);
+      overflow = nrows > kFarRowCap;
+      if (!overflow) {
+        for (int i = lane; i < nrows; i += 32) {
+          fs.xlo[i] = ford(FLT_MAX);
+          fs.xhi[i] = ford(-FLT_MAX);
+        }
+        __syncwarp();
+        if (mine) {
+          // this lane's rows: where its ball reaches the grid's x range, in the rectangle
+          const float rx2 = r2 - dxg * dxg;
+          int z0 = k0, z1 = k1;
+          clip_reach(rx2, q.tz, g.oz, g.inv_h, h, g.dz, z0, z1);
+          for (int kz = z0; kz <= z1; ++kz) {
+            const float gz = axis_gap(kz, q.tz, g.oz, h);
+            const float gz2 = gz * gz;
+            int y0 = j0, y1 = j0 + nyr - 1;
+            clip_reach(rx2 - gz2, q.ty, g.oy, g.inv_h, h, g.dy, y0, y1);
+            for (int jy = y0; jy <= y1; ++jy) {
+              const float gy = axis_gap(jy, q.ty, g.oy, h);
+              const float rem = r2 - fmaf(gy, gy, gz2);
+              if (rem >= 0.0f) {
+                const float rx = (rem > 0.0f ? rem * rsqrtf(rem) * 1.0001f : 0.0f) + kCellMargin * h;
+                const float xa = fmaxf(q.tx - rx, q.lox), xb = fminf(q.tx + rx, q.hix);
+                if (xa <= xb) {
+                  const int row = (kz - k0) * nyr + (jy - j0);
+                  atomicMin(&fs.xlo[row], ford(xa));
+                  atomicMax(&fs.xhi[row], ford(xb));
+                }
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+      int npts = 0;
+      for (int rb = 0; rb < nrows && !overflow; rb += 32) {
+        const int rr = rb + lane;
+        int base = 0, n = 0;
+        if (rr < nrows) {
+          const int kz = k0 + rr / nyr, jy = j0 + rr % nyr;
+          const float xa = fdeord(fs.xlo[rr]), xb = fdeord(fs.xhi[rr]);
+          if (xa <= xb && xb >= g.minx && xa <= g.maxx) {
+            const int c0 = cell_coord(xa, g.ox, g.inv_h, g.dx), c1 = cell_coord(xb, g.ox, g.inv_h, g.dx);
+            const int rowbase = (kz * g.dy + jy) * g.dx;
+            base = __ldg(S.cell_start + FOMO_IDX(rowbase + c0, cell_entries(g), kSiteCellStart));
+            n = __ldg(S.cell_start + FOMO_IDX(rowbase + c1 + 1, cell_entries(g), kSiteCellStart)) - base;
+          }
+        }
+        // the rows' points, 32 per round, each tested by every pending lane
+        const int incl = warp_incl_scan(n);
+        const int excl = incl - n;
+        const int total = __shfl_sync(kFull, incl, 31);
+        npts += total;
+        if (npts > kFarMaxPts) {
+          overflow = true;
+          break;
+        }
+        for (int ib = 0; ib < total; ib += 32) {
+          const int i = ib + lane;
+          const int own = warp_owner(incl, i) & 31;
+          const int ob = __shfl_sync(kFull, base, own), oe = __shfl_sync(kFull, excl, own);
+          if (i < total) {
+            const int p = ob + (i - oe);
+            fs.pt[lane] = __ldg(S.pts + FOMO_IDX(p, S.n, kSitePts));
+            fs.pp[lane] = p;
+          }
+          __syncwarp();
+          const int cn = min(32, total - ib);
+          if (mine)
+            for (int k = 0; k < cn; ++k) scan_point<false>(fs.pt[k], fs.pp[k], q, 0.0f, best, second, bpos, borig, bD);
+          __syncwarp();  // the round's points are rewritten by the next
+        }
+      }
+    }
+    if (overflow) break;
+    // found: the best point lies inside the ball, which was gathered whole;
+    // a near-tie (FP64 re-rank) is left to the lane walk
+    const bool found = mine && best < FLT_MAX && best <= r2 * (1.0f - 2.0f * kRelPrune);
+    const bool tie = found && second <= best * (1.0f + kRelTie);
+    if (found && !tie) {
+      pos = bpos;
+      orig = borig;
+    }
+    solved |= __ballot_sync(kFull, found && !tie);
+    margin2 *= 4.0f;
+    if (mine && !found) r2 = best < FLT_MAX ? best * (1.0f + 1e-4f) : L2 + margin2;
+    pend = __ballot_sync(kFull, mine && !found);
+    __syncwarp();  // the lanes' balls are rewritten by the next gather
+  }
+  return solved;
+}
+
+// The far pass over the deferred records the search listed (a.far_list, read
+// after march_split), a warp per record: each flagged half with at least
+// kFarMin samples left is searched by far_half.  The neighbours go to the
+// position buffer and the record keeps the samples still open, for
+// march_deferred.
+__global__ void __launch_bounds__(kThreads, kMinCtasFar) march_far(MarchArgs a, const double3* __restrict__ ktab,
+                                                                   int ktab_stride, int kind) {
+  __shared__ FarSmem fsm[kWarps];
+  const int w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  // the records the search flagged, listed by their slots
+  const int64_t nlist = min((int64_t)a.counter[kCtrFar], a.deferred_cap);
+  if (!a.far_list || nlist == 0) return;
+  for (;;) {
+    // 32 list entries per grab (one atomic per warp and batch); their records one after the other
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(a.counter + kCtrFarHead, 32ull);
+    base = __shfl_sync(kFull, base, 0);
+    if ((int64_t)base >= nlist) return;
+    const int64_t kk = (int64_t)base + lane;
+    long long mslot = -1;
+    DeferredRec mrec = make_uint4(0u, 0u, 0u, 0u);
+    if (kk < nlist) {
+      mslot = a.far_list[FOMO_IDX(kk, a.deferred_cap, kSiteDeferred)];
+      mrec = a.deferred[FOMO_IDX(mslot, a.deferred_cap, kSiteDeferred)];
+    }
+    unsigned todo = __ballot_sync(kFull, mslot >= 0);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1u;
+      const long long slot = __shfl_sync(kFull, mslot, src);
+      DeferredRec rec;
+      rec.x = __shfl_sync(kFull, mrec.x, src);
+      rec.y = __shfl_sync(kFull, mrec.y, src);
+      rec.z = __shfl_sync(kFull, mrec.z, src);
+      rec.w = __shfl_sync(kFull, mrec.w, src);
+      RayCtx r;
+      if (!ray_of_item(a, ktab, ktab_stride, (int64_t)rec.x, r)) continue;  // records come from real rays only
+#pragma unroll 1
+      for (int hh = 0; hh < 2; ++hh) {
+        unsigned mask = hh ? rec.w : rec.z;
+        if (!(rec.y & (hh ? kRecFar1 : kRecFar0)) || __popc(mask) < kFarMin) continue;
+        const int ks = (int)(rec.y & kRecS0) + 32 * hh + lane;
+        const bool act = ((mask >> lane) & 1u) && ks < r.nz;
+        BoxQ q = {};
+        if (act) q = exact_box(r, ks);
+        int pos = -1, orig = -1;
+        const unsigned solved = far_half(a.snap, q, act, fsm[w], pos, orig) & mask;
+        if (act && ((solved >> lane) & 1u))
+          store_deferred<true>(a, r, ks, kind, pos, orig, ktab_stride, nullptr, nullptr);
+        if (a.stats && lane == 0) {
+          atomicAdd(a.stats + kStatFarGroups, 1ull);
+          atomicAdd(a.stats + kStatFar, (unsigned long long)__popc(solved));
+        }
+        mask &= ~solved;
+        if (hh)
+          rec.w = mask;
+        else
+          rec.z = mask;
+      }
+      if (lane == 0) a.deferred[FOMO_IDX(slot, a.deferred_cap, kSiteDeferred)] = rec;
+    }
+  }
+}
+
 // Phase 1 of march_deferred: samples [0, nsamp) of the staged records, one
 // per lane, each searched by its lane; results staged in sp / sv.  With
 // BUDGET (a short queue: latency matters), a sample in dense cells or over the
@@ -1720,7 +1990,7 @@ __device__ __forceinline__ void deferred_search(const MarchArgs& a, int kind, in
   for (int t0 = 0; t0 < nsamp; t0 += 32) {
     const int t = t0 + lane;
     const int own = warp_owner(incl, start + t) & 31;  // the record lane holding flattened sample t
-    const unsigned oy = __shfl_sync(kFull, rec.y, own);
+    const unsigned oy = __shfl_sync(kFull, rec.y & kRecS0, own);
     const unsigned oz = __shfl_sync(kFull, rec.z, own), ow = __shfl_sync(kFull, rec.w, own);
     const int oe = __shfl_sync(kFull, excl, own);
     const RayCtx r = shfl_ray(mine, own);
@@ -1980,6 +2250,8 @@ cudaError_t launch_march(const MarchArgs& a, const double3* ktab, int ktab_strid
     mark(kKSearch);
     if (e == cudaSuccess) e = launch_queue(march_split<true>, a, ktab, ktab_stride, sm_count, s, kind);
     mark(kKSplit);
+    if (e == cudaSuccess) e = launch_queue(march_far, a, ktab, ktab_stride, sm_count, s, kind);
+    mark(kKFar);
     if (e == cudaSuccess) e = launch_queue(march_deferred<true>, a, ktab, ktab_stride, sm_count, s, kind);
     mark(kKDeferred);
     if (e == cudaSuccess && a.hard_cap > 0) e = launch_queue(march_hard<true>, a, ktab, ktab_stride, sm_count, s, kind);

@@ -775,10 +775,12 @@ int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* 
     // entries, the launch marching in item chunks beyond that
     G.npos_items = 0;
     G.o_npos = 0;
+    G.o_far = 0;
     if (G.method != FOMO_METHOD_PROJECTION) {
       const int64_t cap_items = std::max<int64_t>(1, ctx->npos_cap / G.maxnz);
       G.npos_items = std::min<int64_t>(items, cap_items);
       G.o_npos = L.take(sizeof(int32_t) * (size_t)G.npos_items * G.maxnz);
+      G.o_far = L.take(sizeof(int32_t) * (size_t)G.deferred_cap);
     }
     G.o_s2 = G.method == FOMO_METHOD_THOMSON ? L.take(sizeof(float) * (size_t)G.nv * snap.n) : 0;
   }
@@ -944,6 +946,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.counter = reinterpret_cast<unsigned long long*>(db + G.o_ctr);
     a.deferred = reinterpret_cast<DeferredRec*>(db + G.o_def);
     a.deferred_cap = G.deferred_cap;
+    a.far_list = G.o_far ? reinterpret_cast<int32_t*>(db + G.o_far) : nullptr;
     a.hard = reinterpret_cast<uint2*>(db + G.o_hard);
     a.hard_cap = G.hard_cap;
     a.npos = G.o_npos ? reinterpret_cast<int32_t*>(db + G.o_npos) : nullptr;

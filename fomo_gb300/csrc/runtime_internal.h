@@ -98,6 +98,7 @@ struct PlanGroup {
   int vbase = 0;
   size_t o_views = 0, o_lines = 0, o_off = 0, o_nnp = 0, o_lam = 0, o_ktab = 0, o_xy = 0, o_ctr = 0, o_s2 = 0;
   size_t o_def = 0;          // deferred-sample records
+  size_t o_far = 0;          // slots of the records flagged for the far pass (with a neighbour buffer), or 0
   std::vector<std::pair<float*, size_t>> zero_outs;  // projection outputs to clear before the scatter
   int64_t deferred_cap = 0;  // records: one per segment of every work item
   size_t o_hard = 0;

@@ -118,7 +118,9 @@ size_t request_cost(const fomo_request& q) {
   return cube_elems(q) * sizeof(float) + (size_t)q.nz * 24 + (size_t)(q.nx + q.ny) * 8 + 64 * 1024 +
          rays * (size_t)((q.nz + 63) / 64) * sizeof(DeferredRec) +
          (size_t)hard_capacity((int64_t)rays, q.nz) * sizeof(uint2) +
-         (q.method != FOMO_METHOD_PROJECTION ? rays * (size_t)q.nz * sizeof(int32_t) : 0);  // neighbour buffer
+         (q.method != FOMO_METHOD_PROJECTION  // neighbour buffer and far-pass list
+              ? rays * (size_t)q.nz * sizeof(int32_t) + rays * (size_t)((q.nz + 63) / 64) * sizeof(int32_t)
+              : 0);
 }
 
 // Requests `ids` of slot sl are complete (their cubes are in pinned staging);

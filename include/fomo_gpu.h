@@ -261,7 +261,8 @@ int fomo_last_march_ms(fomo_ctx* ctx, float* ms);
 #define FOMO_KERNEL_HARD 3      /* deferred samples over a lane's budget, one warp each */
 #define FOMO_KERNEL_EMISSION 4  /* emission pass: binning from the stored neighbours */
 #define FOMO_KERNEL_FUSED 5     /* fused search + emission (the no-allocation path) */
-#define FOMO_KERNEL_COUNT 6
+#define FOMO_KERNEL_FAR 6       /* deferred samples of a record searched together, one warp per 32 */
+#define FOMO_KERNEL_COUNT 7
 #define FOMO_COUNTER_SEGMENTS 0      /* 64-sample segments searched */
 #define FOMO_COUNTER_CANDIDATES 1    /* candidates gathered */
 #define FOMO_COUNTER_ROWS 2          /* cell rows visited by the gather */
@@ -279,7 +280,9 @@ int fomo_last_march_ms(fomo_ctx* ctx, float* ms);
 #define FOMO_COUNTER_HARD 14         /* deferred samples searched by a whole warp */
 #define FOMO_COUNTER_RUNS 15         /* runs of equal neighbours binned by the spectral emission pass */
 #define FOMO_COUNTER_EX2 16          /* ex2 evaluations of the spectral emission pass */
-#define FOMO_COUNTER_COUNT 17
+#define FOMO_COUNTER_FAR_GROUPS 17   /* record halves searched together by the far pass */
+#define FOMO_COUNTER_FAR 18          /* deferred samples the far pass resolved */
+#define FOMO_COUNTER_COUNT 19
 int fomo_set_profiling(fomo_ctx* ctx, int kernel_timing, int counters);
 /* The last direct render's kernel times (ms) summed per kind (kernel_ms[k] for
  * FOMO_KERNEL_k, k < nk), and the counters accumulated since they were turned
