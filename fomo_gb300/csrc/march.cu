@@ -1792,18 +1792,20 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
     const bool mine = (pend >> lane) & 1u;
     float best = FLT_MAX, second = FLT_MAX;
     int bpos = -1, borig = -1;
-    double bD = DBL_MAX;
-    // the rows this lane's ball reaches: the (y, z) disc where it meets the
-    // grid's x range, within the box
+    // the rows this lane's ball reaches, within the box: a point of the grid
+    // lies at least the target's distance to the points' bounding box away
+    // along each axis, so the ball's y extent there is sqrt(r^2 - dx^2 - dz^2)
+    // and its z extent sqrt(r^2 - dx^2 - dy^2), dx, dy, dz those distances
     float ylo = FLT_MAX, yhi = -FLT_MAX, zlo = FLT_MAX, zhi = -FLT_MAX;
     if (mine) {
-      const float rho2 = r2 - dxg * dxg;
-      if (rho2 >= 0.0f) {
-        const float rho = (rho2 > 0.0f ? rho2 * rsqrtf(rho2) * 1.0001f : 0.0f) + kCellMargin * h;
-        ylo = fmaxf(q.ty - rho, q.loy);
-        yhi = fminf(q.ty + rho, q.hiy);
-        zlo = fmaxf(q.tz - rho, q.loz);
-        zhi = fminf(q.tz + rho, q.hiz);
+      const float ry2 = r2 - fmaf(dzg, dzg, dxg * dxg), rz2 = r2 - fmaf(dyg, dyg, dxg * dxg);
+      if (ry2 >= 0.0f && rz2 >= 0.0f) {
+        const float ry = (ry2 > 0.0f ? ry2 * rsqrtf(ry2) * 1.0001f : 0.0f) + kCellMargin * h;
+        const float rz = (rz2 > 0.0f ? rz2 * rsqrtf(rz2) * 1.0001f : 0.0f) + kCellMargin * h;
+        ylo = fmaxf(q.ty - ry, q.loy);
+        yhi = fminf(q.ty + ry, q.hiy);
+        zlo = fmaxf(q.tz - rz, q.loz);
+        zhi = fminf(q.tz + rz, q.hiz);
       }
     }
     ylo = warp_min(ylo);
@@ -1830,7 +1832,7 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
           // this lane's rows: where its ball reaches the grid's x range, in the rectangle
           const float rx2 = r2 - dxg * dxg;
           int z0 = k0, z1 = k1;
-          clip_reach(rx2, q.tz, g.oz, g.inv_h, h, g.dz, z0, z1);
+          clip_reach(rx2 - dyg * dyg, q.tz, g.oz, g.inv_h, h, g.dz, z0, z1);
           for (int kz = z0; kz <= z1; ++kz) {
             const float gz = axis_gap(kz, q.tz, g.oz, h);
             const float gz2 = gz * gz;
@@ -1854,11 +1856,13 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
         __syncwarp();
       }
       int npts = 0;
+      const float inv_nyr = nyr > 0 ? 1.0f / (float)nyr : 0.0f;
       for (int rb = 0; rb < nrows && !overflow; rb += 32) {
         const int rr = rb + lane;
         int base = 0, n = 0;
         if (rr < nrows) {
-          const int kz = k0 + rr / nyr, jy = j0 + rr % nyr;
+          int ry;
+          const int kz = k0 + row_div(rr, nyr, inv_nyr, ry), jy = j0 + ry;
           const float xa = fdeord(fs.xlo[rr]), xb = fdeord(fs.xhi[rr]);
           if (xa <= xb && xb >= g.minx && xa <= g.maxx) {
             const int c0 = cell_coord(xa, g.ox, g.inv_h, g.dx), c1 = cell_coord(xb, g.ox, g.inv_h, g.dx);
@@ -1887,8 +1891,26 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
           }
           __syncwarp();
           const int cn = min(32, total - ib);
-          if (mine)
-            for (int k = 0; k < cn; ++k) scan_point<false>(fs.pt[k], fs.pp[k], q, 0.0f, best, second, bpos, borig, bD);
+          if (mine) {
+            // every point of the round against this lane's box and best (the
+            // same test as scan_point); four at a time, their distances independent
+#pragma unroll 4
+            for (int k = 0; k < cn; ++k) {
+              const float4 v = fs.pt[k];
+              if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+                const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+                const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                if (d < best) {
+                  second = best;
+                  best = d;
+                  bpos = fs.pp[k];
+                  borig = __float_as_int(v.w);
+                } else if (d < second) {
+                  second = d;
+                }
+              }
+            }
+          }
           __syncwarp();  // the round's points are rewritten by the next
         }
       }
