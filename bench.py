@@ -30,6 +30,11 @@ serving    : Poisson streams of mixed requests (200/s, and 400/s and 800/s above
 --impl reference runs the reference's CPU algorithm (the oracle port; the
 reference's own build needs Boost/GSL, absent on the GPU host) on a bounded
 sample of the batched workload and prints the same metric.
+
+--profile-case, --c4-case and --far-case are not bench lines: a small
+direct-launch batch for ncu captures, the 8M-point flux-rope renders (six DN
+channels, Thomson on and off the equator) with per-kernel times, and the
+off-equator Thomson render at 512^2 for an ncu capture of the far pass.
 """
 
 from __future__ import annotations
@@ -649,6 +654,63 @@ def run_profile_case(args):
                           "counters": counters, "tuned": tuned}))
 
 
+def run_rope_cases(args):
+    """The 8,388,608-point flux rope (80 % in a twisted rope, 20 % uniform
+    background; fomo_gb300.synth.flux_rope_snapshot), rendered directly with
+    per-kernel CUDA-event timing after warm-up renders, one JSON line.
+
+    --c4-case: six broadband DN channels at 1024 x 1024 px x 1024 LOS samples
+    (l = 0.6, b = 0.35 rad, one batch), then the rope moved to 1.5 solar radii
+    rendered in Thomson pB at 1024 x 1024 x 1024, l = 0.2, b = 0 and b = 0.3
+    rad (200-pixel boxes away from the equator).
+    --far-case: only the off-equator Thomson render, at 512 x 512 x 1024, with
+    the march counters on the last render (a small case for an ncu capture of
+    march_far: three warm-up renders, then the measured one)."""
+    import torch
+
+    import fomo_gb300 as fg
+    from fomo_gb300 import synth
+    dev = torch.device("cuda", 0)
+    out = {}
+    n = 8 * 1024 * 1024
+    with fg.Context(0) as ctx:
+        if args.c4_case:
+            s = synth.flux_rope_snapshot(n, seed=4)
+            sid = ctx.snapshot(s)
+            chans = (94, 131, 171, 193, 211, 335)
+            tids = [ctx.table(synth.broadband_table(c, peak_logT=5.8 + 0.15 * k)) for k, c in enumerate(chans)]
+            reqs = [ctx.request(sid, t, fg.METHOD_NN, 1024, 1024, 1024, 1, 0.6, 0.35, 1e5) for t in tids]
+            outs = [torch.empty((1024, 1024, 1), dtype=torch.float32, device=dev) for _ in reqs]
+            ptrs = [o.data_ptr() for o in outs]
+            ctx.set_profiling(kernel_timing=True)
+            for _ in range(3):
+                ctx.render_batch_device(reqs, ptrs)
+                ctx.synchronize()
+                km, _ = ctx.profile_read()
+            out["six_dn_channels_1024"] = {"march_ms": ctx.last_march_ms(), "kernel_ms": km}
+            ctx.set_profiling(False, False)
+            ctx.drop_snapshot(sid)
+        ts = synth.flux_rope_snapshot(n, seed=5, center=(1.5 * 695.7, 0.0, 0.0))
+        tsid = ctx.snapshot(ts)
+        cases = [(0.0, 1024), (0.3, 1024)] if args.c4_case else [(0.3, 512)]
+        for b, px in cases:
+            q = ctx.request(tsid, 0, fg.METHOD_THOMSON, px, px, 1024, 1, 0.2, b, 1e5)
+            o = torch.empty((px, px, 1), dtype=torch.float32, device=dev)
+            for _ in range(3):
+                ctx.render_device(q, o.data_ptr())
+                ctx.synchronize()
+            ctx.set_profiling(kernel_timing=True, counters=args.far_case)
+            ctx.render_device(q, o.data_ptr())
+            ctx.synchronize()
+            km, cn = ctx.profile_read()
+            ctx.set_profiling(False, False)
+            rec = {"march_ms": ctx.last_march_ms(), "kernel_ms": km}
+            if args.far_case:
+                rec["counters"] = {k: cn[k] for k in ("deferred", "far_groups", "far")}
+            out[f"thomson_{px}_b{b}"] = rec
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -660,11 +722,15 @@ def main():
     ap.add_argument("--profile-case", action="store_true", help="small direct-launch case for ncu captures")
     ap.add_argument("--no-breakdown", action="store_true", help="profile case without the timing/counter launches")
     ap.add_argument("--tune-cache", default=None, help="profile case: autotuner cache file (written when absent)")
+    ap.add_argument("--c4-case", action="store_true", help="8M-point flux rope: 6 DN channels and Thomson at 1024^2")
+    ap.add_argument("--far-case", action="store_true", help="8M-point rope, off-equator Thomson at 512^2 (ncu)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.profile_case:
         run_profile_case(args)
+    elif args.c4_case or args.far_case:
+        run_rope_cases(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
