@@ -166,6 +166,7 @@ cudaError_t launch_aabb(const float* x, const float* y, const float* z, int64_t 
                         cudaStream_t s);
 cudaError_t launch_bin_points(const float* x, const float* y, const float* z, int64_t n, GridParams g,
                               int* cell_of, int* counts, cudaStream_t s);
+cudaError_t launch_count_empty(const int* counts, int64_t ncells, unsigned long long* empty, cudaStream_t s);
 cudaError_t launch_exclusive_scan(const int* in, int* out, int64_t count, int* scratch, int64_t scratch_ints,
                                   cudaStream_t s);
 int64_t exclusive_scan_scratch_ints(int64_t count);

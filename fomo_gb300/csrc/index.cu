@@ -222,6 +222,23 @@ cudaError_t launch_bin_points(const float* x, const float* y, const float* z, in
   return cudaGetLastError();
 }
 
+// The number of cells whose count is 0 (added to *empty, zeroed by the caller).
+__global__ void count_empty_kernel(const int* __restrict__ counts, int64_t ncells, unsigned long long* empty) {
+  unsigned long long k = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ncells; i += (int64_t)gridDim.x * blockDim.x)
+    k += counts[i] == 0 ? 1ull : 0ull;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+  if ((threadIdx.x & 31) == 0 && k) atomicAdd(empty, k);
+}
+
+cudaError_t launch_count_empty(const int* counts, int64_t ncells, unsigned long long* empty, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(empty, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  count_empty_kernel<<<grid_blocks(ncells, 256), 256, 0, s>>>(counts, ncells, empty);
+  return cudaGetLastError();
+}
+
 int64_t exclusive_scan_scratch_ints(int64_t count) { return (count + kScanTile - 1) / kScanTile + 1; }
 
 cudaError_t launch_exclusive_scan(const int* in, int* out, int64_t count, int* scratch, int64_t scratch_ints,

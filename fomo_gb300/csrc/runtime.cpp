@@ -284,6 +284,8 @@ GridParams choose_grid(const float* mn, const float* mx, int64_t n, double ppc) 
   return g;
 }
 
+constexpr double kUniformEmpty = 0.10;  // empty-cell share below which a cloud counts as uniform
+
 int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec* out) {
   cudaStream_t s = ctx->stream;
   // staging: 8 arrays of n floats (z may be absent -> zeros, as nn:82 for 2-D data)
@@ -330,7 +332,41 @@ int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec
     dev_free(ctx, bits);
     return set_err(ctx, FOMO_EINVAL, "snapshot coordinates contain NaN or infinity");
   }
-  GridParams g = choose_grid(mn, mx, n, ctx->cell_occupancy);
+  // Grid cell size.  A cloud that is close to uniform at the cell scale (fewer
+  // than kUniformEmpty of the cells empty at 2 points per cell) gets cells of 1
+  // point: its searches then load fewer points per candidate and its ring
+  // walks are shorter (the 2M-point loop's batched render: 4 % faster).  A
+  // clustered cloud keeps 2 points per cell: finer cells would leave its sparse
+  // regions' walks crossing more empty cells (8M-point flux rope: 17-26 %
+  // slower at 1 point per cell).  FOMO_CELL_OCCUPANCY sets the occupancy and
+  // skips the choice.
+  double ppc = ctx->cell_occupancy;
+  if (!ctx->occupancy_set && n >= 1024) {
+    const GridParams g2 = choose_grid(mn, mx, n, 2.0);
+    const int64_t nc2 = (int64_t)g2.dx * g2.dy * g2.dz;
+    int* t2 = nullptr;
+    rc = dev_alloc(ctx, reinterpret_cast<void**>(&t2), sizeof(int) * (size_t)(n + nc2));
+    if (rc) {
+      dev_free(ctx, stage);
+      dev_free(ctx, bits);
+      return rc;
+    }
+    unsigned long long hempty = 0;
+    unsigned long long* dempty = reinterpret_cast<unsigned long long*>(bits);
+    e = cudaMemsetAsync(t2 + n, 0, sizeof(int) * (size_t)nc2, s);
+    if (e == cudaSuccess) e = launch_bin_points(a[0], a[1], a[2], n, g2, t2, t2 + n, s);
+    if (e == cudaSuccess) e = launch_count_empty(t2 + n, nc2, dempty, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hempty, dempty, sizeof(hempty), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dev_free(ctx, t2);
+    if (e != cudaSuccess) {
+      dev_free(ctx, stage);
+      dev_free(ctx, bits);
+      return cuda_err(ctx, e, "snapshot cell statistics");
+    }
+    ppc = (double)hempty < kUniformEmpty * (double)nc2 ? 1.0 : 2.0;
+  }
+  GridParams g = choose_grid(mn, mx, n, ppc);
   const int64_t ncells = (int64_t)g.dx * g.dy * g.dz;
   const int64_t scan_count = ncells + 1;
   const int64_t scr = exclusive_scan_scratch_ints(scan_count);
@@ -1102,7 +1138,10 @@ int fomo_ctx_create(int device, size_t hbm_budget_bytes, fomo_ctx** out) {
   }
   if (const char* co = std::getenv("FOMO_CELL_OCCUPANCY")) {
     const double v = std::atof(co);  // target points per grid cell of the snapshots built afterwards
-    if (v >= 0.25 && v <= 64.0) ctx->cell_occupancy = v;
+    if (v >= 0.25 && v <= 64.0) {
+      ctx->cell_occupancy = v;
+      ctx->occupancy_set = true;
+    }
   }
   if (const char* fa = std::getenv("FOMO_INJECT_ALLOC_FAILURE")) ctx->fail_alloc_at = std::atol(fa);
   const char* tm = std::getenv("FOMO_TIME_MARCH");

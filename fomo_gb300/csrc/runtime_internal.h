@@ -159,7 +159,8 @@ struct fomo_ctx {
   fomo::ScratchSet scratch;  // descriptors, per-view tables, Thomson sin^2 chi
   fomo::Arena out_arena;     // device cubes of host-output renders
   std::vector<fomo::ViewReadback> view_readback;
-  double cell_occupancy = 2.0;  // target points per grid cell
+  double cell_occupancy = 2.0;  // target points per grid cell (FOMO_CELL_OCCUPANCY)
+  bool occupancy_set = false;   // set explicitly: no per-snapshot choice (see build_snapshot)
   int64_t npos_cap = int64_t(1) << 31;  // neighbour-buffer entries per launch (FOMO_NPOS_CAP): 8 GiB
   long fail_alloc_at = 0;  // FOMO_INJECT_ALLOC_FAILURE: this allocation (1-based) fails, for error-path tests
   long alloc_count = 0;
