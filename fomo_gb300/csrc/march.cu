@@ -89,10 +89,10 @@ constexpr int kSeg = 64;              // LOS samples per segment (two per lane)
 constexpr int kSegCap = 176;          // candidates per segment (sized so that 7 search CTAs fit an SM)
 constexpr int kMaxRows = 4096;        // cell rows of a segment's capsule beyond which it is deferred
 constexpr float kRScaleDefault = 0.9f;  // gather radius in local point spacings (MarchArgs::rscale when set)
-// Far pass (march_far): samples two cells or more off the points' bounding box,
+// Far pass (march_far): samples half a cell or more off the points' bounding box,
 // kFarMin or more of them in a half record, searched together by a warp.
-constexpr int kFarMin = 8;          // far samples a half needs (fewer: the lane walks of march_deferred)
-constexpr float kFarOut2 = 4.0f;    // squared distance, in cells, off the points' bounding box of a far sample
+constexpr int kFarMin = 4;          // far samples a half needs (fewer: the lane walks of march_deferred)
+constexpr float kFarOut2 = 0.25f;   // squared distance, in cells, off the points' bounding box of a far sample
 constexpr float kFarBox = 8.0f;     // box half-width, in cells, of the views the far pass takes (narrower: lane walks)
 constexpr int kFarIters = 4;        // gathers per half
 constexpr int kFarMaxPts = 1024;    // points of a gather beyond which the half is left to march_deferred
@@ -861,7 +861,7 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
     const int64_t slot = over ? a.deferred_cap - 1 - (int64_t)k : (int64_t)k;
     // the halves the far pass may take, in views whose boxes reach kFarBox
     // cells or more from their target: kFarMin or more deferred samples, the
-    // whole half two cells or more off the points' bounding box (the box of
+    // whole half half a cell or more off the points' bounding box (the box of
     // the half's stretch of the segment against the points' box)
     unsigned flags = 0u;
     bool listed = false;
@@ -1721,7 +1721,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
 
 // ---------------------------------------------------------------------------
 // Far samples: the deferred samples of one half of a record (up to 32
-// consecutive LOS samples of one ray, lane = sample) that lie two cells or
+// consecutive LOS samples of one ray, lane = sample) that lie half a cell or
 // more outside the points' bounding box, searched together; the search pass
 // flags the halves that hold kFarMin of them or more.  Such samples lie away
 // from the points (wide boxes off the cloud, as Thomson's far from the
@@ -1784,7 +1784,7 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
   const float L2 = fmaf(dzg, dzg, fmaf(dyg, dyg, dxg * dxg));
   float margin2 = 4.0f * h * h;  // the ball's margin beyond that bound, squared: two cells at first
   float r2 = L2 + margin2;
-  // far samples only (two cells or more off the points): near and inside the
+  // far samples only (half a cell or more off the points): near and inside the
   // cloud the balls' union holds too many points for every lane to test
   unsigned pend = __ballot_sync(kFull, in_grid && L2 >= kFarOut2 * h * h);
   if (__popc(pend) < kFarMin) pend = 0;
