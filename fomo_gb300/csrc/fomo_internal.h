@@ -25,7 +25,10 @@ struct SnapDev {
   const float4* vel;    // sorted: vx, vy, vz (m/s), 0
   const int* cell_start;  // dx*dy*dz + 1 slots
   GridParams g;
+  const float* blk;     // per block of kBlockCells^3 cells: its points' min x, y, z and max x, y, z
+  int bdx, bdy, bdz;    // blocks per axis
 };
+constexpr int kBlockCells = 8;  // cells per block edge (per-block bounding boxes of a snapshot)
 
 // ---------------------------------------------------------------------------
 // One view (l, b) of one snapshot.  Host fills the first block (trig values
@@ -47,6 +50,8 @@ struct ViewDesc {
   int ray_tile_w, ray_tile_h;  // ray tile shape for the march work order
   // ---- device-filled by the extents + finalize kernels
   unsigned long long ext_bits[6];  // order-preserving encodings for atomic min/max
+  int bnd[6];                // per rotated axis: the largest lower bound of a block's values and the smallest
+                             // upper bound (order-preserving float encodings), which bound the extremes
   double minx, maxx, miny, maxy, minz, maxz;
   double md;                 // maxdistance
   double deltaz;
@@ -166,6 +171,8 @@ cudaError_t launch_aabb(const float* x, const float* y, const float* z, int64_t 
                         cudaStream_t s);
 cudaError_t launch_bin_points(const float* x, const float* y, const float* z, int64_t n, GridParams g,
                               int* cell_of, int* counts, cudaStream_t s);
+cudaError_t launch_block_bounds(const float4* pts, const int* cell_start, GridParams g, int bdx, int bdy, int bdz,
+                                float* blk, cudaStream_t s);
 cudaError_t launch_count_empty(const int* counts, int64_t ncells, unsigned long long* empty, cudaStream_t s);
 cudaError_t launch_exclusive_scan(const int* in, int* out, int64_t count, int* scratch, int64_t scratch_ints,
                                   cudaStream_t s);

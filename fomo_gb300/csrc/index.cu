@@ -10,6 +10,7 @@
 // original index so the layout is deterministic.  The index is built once per
 // snapshot and stays resident.
 #include <cuda_runtime.h>
+#include <float.h>
 #include <stdint.h>
 
 #include "fomo_device.cuh"
@@ -219,6 +220,53 @@ cudaError_t launch_aabb(const float* x, const float* y, const float* z, int64_t 
 cudaError_t launch_bin_points(const float* x, const float* y, const float* z, int64_t n, GridParams g, int* cell_of,
                               int* counts, cudaStream_t s) {
   bin_kernel<<<grid_blocks(n, 256), 256, 0, s>>>(x, y, z, n, g, cell_of, counts);
+  return cudaGetLastError();
+}
+
+// One warp per block of kBlockCells^3 cells: the bounding box of its points
+// (min x, y, z, max x, y, z), from its rows' point ranges; an empty block gets
+// min = FLT_MAX, max = -FLT_MAX.  The view set-up bounds each view's extents
+// by these boxes (view.cu).
+__global__ void block_bounds_kernel(const float4* __restrict__ pts, const int* __restrict__ cell_start, GridParams g,
+                                    int bdx, int bdy, int bdz, float* __restrict__ blk) {
+  const int64_t nblk = (int64_t)bdx * bdy * bdz;
+  const int64_t b = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (b >= nblk) return;  // the whole warp
+  const int bx = (int)(b % bdx), by = (int)((b / bdx) % bdy), bz = (int)(b / ((int64_t)bdx * bdy));
+  const int x0 = bx * kBlockCells, x1 = min(x0 + kBlockCells, g.dx) - 1;
+  const int64_t entries = (int64_t)g.dx * g.dy * g.dz + 1;
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int r = lane; r < kBlockCells * kBlockCells; r += 32) {
+    const int cy = by * kBlockCells + r % kBlockCells, cz = bz * kBlockCells + r / kBlockCells;
+    if (cy >= g.dy || cz >= g.dz) continue;
+    const int64_t rowbase = ((int64_t)cz * g.dy + cy) * g.dx;
+    const int p1 = cell_start[FOMO_IDX(rowbase + x1 + 1, entries, kSiteIndexBuild)];
+    for (int p = cell_start[FOMO_IDX(rowbase + x0, entries, kSiteIndexBuild)]; p < p1; ++p) {
+      const float4 v = pts[p];
+      mn[0] = fminf(mn[0], v.x);
+      mn[1] = fminf(mn[1], v.y);
+      mn[2] = fminf(mn[2], v.z);
+      mx[0] = fmaxf(mx[0], v.x);
+      mx[1] = fmaxf(mx[1], v.y);
+      mx[2] = fmaxf(mx[2], v.z);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+      mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+    }
+  if (lane < 6) blk[FOMO_IDX(6 * b + lane, 6 * nblk, kSiteIndexBuild)] = lane < 3 ? mn[lane] : mx[lane - 3];
+}
+
+cudaError_t launch_block_bounds(const float4* pts, const int* cell_start, GridParams g, int bdx, int bdy, int bdz,
+                                float* blk, cudaStream_t s) {
+  const int64_t nblk = (int64_t)bdx * bdy * bdz;
+  const int64_t threads = nblk * 32;
+  block_bounds_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(pts, cell_start, g, bdx, bdy, bdz, blk);
   return cudaGetLastError();
 }
 

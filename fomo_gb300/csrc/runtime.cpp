@@ -387,8 +387,11 @@ int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec
   R.n = n;
   R.ncells = ncells;
   R.g = g;
+  const int bdx = (g.dx + kBlockCells - 1) / kBlockCells, bdy = (g.dy + kBlockCells - 1) / kBlockCells,
+            bdz = (g.dz + kBlockCells - 1) / kBlockCells;
+  const int64_t nblk = (int64_t)bdx * bdy * bdz;
   const size_t resident = sizeof(float4) * 2 * (size_t)n + sizeof(float) * 2 * (size_t)n +
-                          sizeof(int) * (size_t)(ncells + 1);
+                          sizeof(int) * (size_t)(ncells + 1) + sizeof(float) * 6 * (size_t)nblk;
   void* res = nullptr;
   rc = dev_alloc(ctx, &res, resident);
   if (rc) {
@@ -405,6 +408,10 @@ int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec
   R.ne = reinterpret_cast<float*>(R.vel + n);
   R.T = R.ne + n;
   R.cell_start = reinterpret_cast<int*>(R.T + n);
+  R.blk = reinterpret_cast<float*>(R.cell_start + ncells + 1);
+  R.bdx = bdx;
+  R.bdy = bdy;
+  R.bdz = bdz;
   e = cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)(2 * ncells + 1), s);
   if (e == cudaSuccess) e = launch_bin_points(a[0], a[1], a[2], n, g, cell_of, counts, s);
   if (e == cudaSuccess) e = launch_exclusive_scan(counts, R.cell_start, scan_count, scratch, scr, s);
@@ -412,6 +419,7 @@ int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec
     e = launch_scatter(a[0], a[1], a[2], a[5], a[6], a[7], a[3], a[4], n, cell_of, R.cell_start, fill, R.pts, R.vel,
                        R.ne, R.T, s);
   if (e == cudaSuccess) e = launch_sort_cells(R.cell_start, ncells, R.pts, R.vel, R.ne, R.T, s);
+  if (e == cudaSuccess) e = launch_block_bounds(R.pts, R.cell_start, g, bdx, bdy, bdz, R.blk, s);
   unsigned int vbits = 0x7f800000u;
   if (e == cudaSuccess) e = launch_speed_max(R.vel, n, bits, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&vbits, bits, sizeof(vbits), cudaMemcpyDeviceToHost, s);
@@ -435,6 +443,10 @@ SnapDev snap_dev(const SnapRec& r) {
   s.vel = r.vel;
   s.cell_start = r.cell_start;
   s.g = r.g;
+  s.blk = r.blk;
+  s.bdx = r.bdx;
+  s.bdy = r.bdy;
+  s.bdz = r.bdz;
   return s;
 }
 

@@ -38,6 +38,8 @@ struct SnapRec {
   float* ne = nullptr;
   float* T = nullptr;
   int* cell_start = nullptr;
+  float* blk = nullptr;      // per-block bounding boxes (SnapDev::blk)
+  int bdx = 0, bdy = 0, bdz = 0;
   float2* totpol = nullptr;  // Thomson payload, built on first use
   float vmax = 0.0f;         // largest |v| (bounds every Doppler shift)
 };
