@@ -1739,8 +1739,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
 // kFarIters gathers, near-ties and gathers beyond the row or point bounds go
 // on to march_deferred as before.
 // ---------------------------------------------------------------------------
-constexpr int kMinCtasFar = 6;
-
+constexpr int kMinCtasFar = 6;   // 24 warps per SM at <= 80 registers
 constexpr int kFarRowCap = 256;  // rows of a gather's bounding rectangle (beyond: the half is left)
 struct __align__(16) FarSmem {
   float4 pt[32];           // a round of gathered points
