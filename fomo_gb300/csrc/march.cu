@@ -318,6 +318,18 @@ __device__ __forceinline__ void clip_interval(float a, float d, float inv_d, flo
   }
 }
 
+// The gather radius of a segment: rscale local point spacings, capped where
+// no box needs more -- at sqrt(3) times maxdistance widened by the box
+// corners' rounding margin (the largest any sample of the segment takes, its
+// coordinates at most amax), plus a few ulp of the coordinates.  With that
+// margin in the cap, a box smaller than the spacing lies inside the gathered
+// ball whole and an empty one is accepted by the search instead of deferred.
+__device__ __forceinline__ float gather_radius(const MarchArgs& a, const RayCtx& r, float aloc, float amax) {
+  const float md_seg = r.mdf + (amax + r.mdf) * 4.8e-7f + r.mdf * 1.2e-7f;
+  const float cap = fmaf(md_seg * 1.7321f, 1.0001f, amax * 4.8e-7f) * 1.0001f;
+  return fminf(cap, (a.rscale > 0.0f ? a.rscale : kRScaleDefault) * aloc);
+}
+
 struct PartIn {
   float tx[2], ty[2], tz[2];
   bool act[2];
@@ -372,9 +384,9 @@ __device__ __forceinline__ PartOut segment_parts(const MarchArgs& a, const RayCt
     }
     const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
     const float aloc = g.h * spacing_cells(mocc);
-    const float R = fminf(r.mdf * 1.7321f * 1.0001f, (a.rscale > 0.0f ? a.rscale : kRScaleDefault) * aloc);
     const float amax =
         fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
+    const float R = gather_radius(a, r, aloc, amax);
     const float Rg = R * 1.0001f + amax * 2.4e-7f;  // + a few ulp of the coordinates
     const float Rg2 = Rg * Rg * (1.0f + kRelPrune);
     // ---- 1. gather
@@ -650,9 +662,9 @@ __device__ __forceinline__ void segment_search(const MarchArgs& a, const RayCtx&
   }
   const float mocc = fmaxf((float)__reduce_add_sync(kFull, (unsigned)occ) * (1.0f / 32.0f), 0.125f);
   const float aloc = g.h * spacing_cells(mocc);
-  const float R = fminf(r.mdf * 1.7321f * 1.0001f, (a.rscale > 0.0f ? a.rscale : kRScaleDefault) * aloc);
   const float amax =
       fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))), fmaxf(fabsf(az), fabsf(bz)));
+  const float R = gather_radius(a, r, aloc, amax);
   const float Rg = R * 1.0001f + amax * 2.4e-7f;  // + a few ulp of the coordinates
   const float Rg2 = Rg * Rg * (1.0f + kRelPrune);
   // ---- 1. gather
