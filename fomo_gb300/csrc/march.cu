@@ -93,7 +93,7 @@ constexpr float kRScaleDefault = 0.9f;  // gather radius in local point spacings
 // kFarMin or more of them in a half record, searched together by a warp.
 constexpr int kFarMin = 4;          // far samples a half needs (fewer: the lane walks of march_deferred)
 constexpr float kFarOut2 = 0.25f;   // squared distance, in cells, off the points' bounding box of a far sample
-constexpr float kFarBox = 8.0f;     // box half-width, in cells, of the views the far pass takes (narrower: lane walks)
+constexpr float kFarBox = 4.0f;     // box half-width, in cells, of the views the far pass takes (narrower: lane walks)
 constexpr int kFarIters = 4;        // gathers per half
 constexpr int kFarMaxPts = 1024;    // points of a gather beyond which the half is left to march_deferred
 // A deferred record is (work item, first sample of its 64-sample segment with
