@@ -1198,29 +1198,32 @@ constexpr int kDefBatch = 256;  // deferred samples staged per warp between sear
 // Candidate v (sorted position p) against box q: kept when strictly inside;
 // the two best FP32 squared distances, or (EXACT) the smallest FP64 distance
 // within `band`, lowest original index on exact ties.
+// The distance comes first: a point no nearer than the second best (or
+// beyond the band) changes nothing whether it lies in the box or not, so the
+// box test is made only for the others.
 template <bool EXACT>
 __device__ __forceinline__ void scan_point(const float4 v, int p, const BoxQ& q, float band, float& best,
                                            float& second, int& bpos, int& borig, double& bD) {
-  if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-    const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-    const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-    const int o = __float_as_int(v.w);
-    if (!EXACT) {
-      if (d < best) {
-        second = best;
-        best = d;
-        bpos = p;
-        borig = o;
-      } else if (d < second) {
-        second = d;
-      }
-    } else if (d <= band) {
-      const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
-      if (D < bD || (D == bD && o < borig)) {
-        bD = D;
-        borig = o;
-        bpos = p;
-      }
+  const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+  const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  if (!(EXACT ? d <= band : d < second)) return;
+  if (!(v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz)) return;
+  const int o = __float_as_int(v.w);
+  if (!EXACT) {
+    if (d < best) {
+      second = best;
+      best = d;
+      bpos = p;
+      borig = o;
+    } else {
+      second = d;
+    }
+  } else {
+    const double D = exact_dist2(v.x, v.y, v.z, q.tx, q.ty, q.tz);
+    if (D < bD || (D == bD && o < borig)) {
+      bD = D;
+      borig = o;
+      bpos = p;
     }
   }
 }
@@ -1903,20 +1906,21 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
           __syncwarp();
           const int cn = min(32, total - ib);
           if (mine) {
-            // every point of the round against this lane's box and best (the
+            // every point of the round against this lane's best and box (the
             // same test as scan_point); four at a time, their distances independent
 #pragma unroll 4
             for (int k = 0; k < cn; ++k) {
               const float4 v = fs.pt[k];
-              if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
-                const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
-                const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
+              const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              if (d < second && v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz &&
+                  v.z < q.hiz) {
                 if (d < best) {
                   second = best;
                   best = d;
                   bpos = fs.pp[k];
                   borig = __float_as_int(v.w);
-                } else if (d < second) {
+                } else {
                   second = d;
                 }
               }
