@@ -15,14 +15,16 @@
 // section 3.2.4) in an RFC 1952 member with a CRC-32 trailer: any gzip reader
 // returns the same bytes as the uncompressed file.
 #include <algorithm>
+#include <charconv>
 #include <cstdint>
 #include <cstdio>
 #include <iterator>
 #include <fstream>
-#include <iomanip>
 #include <iostream>
 #include <sstream>
 #include <stdexcept>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/FoMo.h"
@@ -81,30 +83,73 @@ bool gzip_file(const std::string& src, const std::string& dst) {
 
 }  // namespace
 
-// The text format.  Floats go through the stream with 8 significant digits,
-// as the reference writes them.
+// One value of the text format's body as the reference's stream writes it at
+// precision 8: the float widened to double, in printf's "%.8g" form in the
+// "C" locale (which std::to_chars with chars_format::general and a precision
+// reproduces exactly), then a space.  At most 15 characters plus the space.
+static char* put_text_value(char* p, char* end, float v) {
+  const std::to_chars_result r = std::to_chars(p, end, (double)v, std::chars_format::general, 8);
+  *r.ptr = ' ';
+  return r.ptr + 1;
+}
+
+// The text format (fomo-io.cpp:26-77).  Its body is one line per point, the
+// reference writes it through the stream one value at a time and flushes
+// every line; here blocks of lines are formatted by several threads at once
+// into memory and written in order, with the same bytes.
 static void write_text(GoftCube& c, const std::string& filename) {
-  std::ofstream out(filename, std::ios::ate);
+  std::ofstream out(filename, std::ios::ate | std::ios::binary);
   if (!out.is_open()) {
     std::cerr << "Unable to write to " << filename << std::endl;
     return;
   }
   const int nvars = c.readnvars(), dim = c.readdim(), ng = c.readngrid();
-  out << "FoMo-" << kVersion << std::endl;
-  out << dim << std::endl << ng << std::endl << nvars << std::endl;
+  out << "FoMo-" << kVersion << '\n';
+  out << dim << '\n' << ng << '\n' << nvars << '\n';
   const std::vector<std::string> units = c.readunit();
   for (int u = 0; u < dim + nvars; ++u) out << units.at(u) << "\t";
-  out << std::endl;
-  out << c.readchiantifile() << std::endl;
-  out << c.readabundfile() << std::endl;
+  out << '\n';
+  out << c.readchiantifile() << '\n';
+  out << c.readabundfile() << '\n';
   const tgrid grid = c.readgrid();
   tvars vars;
   for (int i = 0; i < nvars; ++i) vars.push_back(c.readvar(i));
-  out << std::setprecision(8);
-  for (int j = 0; j < ng; ++j) {
-    for (int i = 0; i < dim; ++i) out << grid[i][j] << " ";
-    for (int i = 0; i < nvars; ++i) out << vars[i][j] << " ";
-    out << std::endl;
+  std::vector<const float*> cols;
+  for (int i = 0; i < dim; ++i) cols.push_back(grid[i].data());
+  for (int i = 0; i < nvars; ++i) cols.push_back(vars[i].data());
+  const size_t ncol = cols.size();
+  const size_t line_max = 16 * ncol + 1;
+  constexpr int kLinesPerBlock = 1 << 15;
+  const int nblocks = (ng + kLinesPerBlock - 1) / kLinesPerBlock;
+  const int nthreads =
+      (int)std::max(1u, std::min({std::thread::hardware_concurrency(), 16u, (unsigned)std::max(nblocks, 1)}));
+  std::vector<std::vector<char>> buf(nthreads, std::vector<char>(line_max * kLinesPerBlock));
+  std::vector<size_t> used(nthreads, 0);
+  auto format = [&](int t, int blk) {
+    char* const b = buf[t].data();
+    char* p = b;
+    char* const end = b + buf[t].size();
+    const int64_t j1 = std::min<int64_t>(ng, (int64_t)(blk + 1) * kLinesPerBlock);
+    for (int64_t j = (int64_t)blk * kLinesPerBlock; j < j1; ++j) {
+      for (size_t i = 0; i < ncol; ++i) p = put_text_value(p, end, cols[i][j]);
+      *p++ = '\n';
+    }
+    used[t] = (size_t)(p - b);
+  };
+  // waves of nthreads blocks: formatted in parallel, written in block order
+  for (int b0 = 0; b0 < nblocks; b0 += nthreads) {
+    const int nb = std::min(nthreads, nblocks - b0);
+    std::vector<std::thread> pool;
+    int t = 1;
+    try {
+      for (; t < nb; ++t) pool.emplace_back(format, t, b0 + t);
+    } catch (const std::system_error&) {
+      // no thread to be had: this one formats the blocks left
+    }
+    for (int u = t; u < nb; ++u) format(u, b0 + u);
+    format(0, b0);
+    for (std::thread& th : pool) th.join();
+    for (int k = 0; k < nb; ++k) out.write(buf[k].data(), (std::streamsize)used[k]);
   }
 }
 

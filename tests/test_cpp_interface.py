@@ -124,6 +124,69 @@ def test_gzip_option_and_delete_option(programs, tmp_path):
     assert read_cube(str(tmp_path / "d.dat.gz"))["body"] == read_cube(src)["body"]
 
 
+def _write_dat(path, cols, dim, units):
+    """A .dat cube (the binary format above) from FP32 columns [dim + nvars][ng]."""
+    with open(path, "wb") as f:
+        f.write(b"FoMo-vtest#")
+        f.write(struct.pack("<iii", dim, cols.shape[1], cols.shape[0] - dim))
+        for s in units + ["table.dat", "/empty"]:
+            f.write(struct.pack("<q", len(s)) + s.encode())
+        f.write(np.ascontiguousarray(cols, np.float32).tobytes())
+
+
+def test_text_writer_formats_every_float_like_the_stream(programs, tmp_path):
+    """The text body is formatted by several threads in blocks of lines; every
+    value must still read as the reference's stream writes it at precision 8,
+    which is the C library's "%.8g" of the float widened to double.  Checked on
+    557,179 lines (18 blocks of 2^15 lines: more than one wave of threads) of
+    random bit patterns of every class (subnormals, normals over the whole
+    exponent range, zeros, infinities, NaNs of either sign) and random values,
+    with the line number as one column so that a block out of order shows."""
+    import ctypes
+    rng = np.random.default_rng(11)
+    ng = 17 * 32768 + 123
+    bits = rng.integers(0, 2 ** 32, ng, dtype=np.uint64).astype(np.uint32)
+    special = np.array([0, 0x80000000, 0x7F800000, 0xFF800000, 0x7FC00000, 0xFFC00000, 0x7F800001, 1, 0x807FFFFF,
+                        0x00800000, 0x7F7FFFFF, 0xFF7FFFFF, 0x3F800000, 0x4B189680], np.uint32)
+    bits[:special.size] = special
+    cols = np.stack([bits.view(np.float32),
+                     (rng.standard_normal(ng) * 10.0 ** rng.integers(-12, 12, ng)).astype(np.float32),
+                     np.arange(ng, dtype=np.float32),
+                     rng.uniform(170.0, 172.0, ng).astype(np.float32)])
+    src = str(tmp_path / "in.dat")
+    _write_dat(src, cols, 3, ["Mm", "Mm", "A", "erg"])
+    out = str(tmp_path / "out.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, "2"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = open(out, "rb").read().decode().split("\n")
+    assert lines[:7] == ["FoMo-" + lines[0][5:], "3", str(ng), "1", "Mm\tMm\tA\terg\t", "table.dat", "/empty"]
+    assert len(lines) == 7 + ng + 1 and lines[-1] == ""
+    libc = ctypes.CDLL(None)
+    buf = ctypes.create_string_buffer(64)
+
+    def printf_g8(v):
+        libc.snprintf(buf, 64, b"%.8g", ctypes.c_double(float(v)))
+        return buf.value.decode()
+
+    with np.errstate(invalid="ignore"):  # the signalling NaNs are quieted, as the C++ widening does
+        vals = cols.T.astype(np.float64)
+    for c in range(4):
+        got = [ln.split(" ")[c] for ln in lines[7:7 + ng]]
+        col = vals[:, c]
+        nan = np.isnan(col)
+        # Python's "%.8g" rounds exactly as the C library does for finite and
+        # infinite values; NaNs (whose sign the C library prints) go through it
+        want = ["%.8g" % v for v in col]
+        for k in np.flatnonzero(nan):
+            want[k] = printf_g8(col[k])
+        bad = [k for k in range(ng) if got[k] != want[k]]
+        assert not bad, (c, [(k, got[k], want[k]) for k in bad[:5]])
+    assert all(ln.endswith(" ") for ln in lines[7:7 + ng])
+    # the C library agrees with Python's formatting on a sample of the finite values
+    for v in vals[:4000, 0][np.isfinite(vals[:4000, 0])]:
+        assert printf_g8(v) == "%.8g" % v
+
+
 def _write_data(path, snap):
     cols = np.stack([snap.x, snap.y, snap.z, snap.n, snap.T, snap.vx, snap.vy, snap.vz], axis=1)
     with open(path, "w") as f:
