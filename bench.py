@@ -16,7 +16,7 @@ plain_*    : the plain single-request GPU render (512x512, 128 bins, 512
              workload's own 256 requests rendered one per call (identical work).
 e2e        : the same batch through the C ABI with pinned host buffers: upload
              the snapshot, build the index, emissivity, render, download every
-             cube, per step (median of 5 steps).
+             cube, per step (median of 9 steps).
 roofline   : the march kernel's algorithmic bytes / its event-timed duration
              against the measured HBM copy bandwidth.
 cpu_baseline: the oracle (C restatement, OpenMP on all host cores) on a bounded
@@ -493,7 +493,7 @@ def run_ours(args):
     e2e_times = []
     h2d = sum(a.numel() * 4 for a in hsnap) + sum(t.G.nbytes + t.logT.nbytes + t.logn.nbytes for t in tables)
     d2h = sum(o.numel() * 4 for o in hout)
-    e2e_steps = 5  # median of 5: host-side copies vary with other jobs on the host
+    e2e_steps = 9  # median of 9: host-side copies vary with other jobs on the host
     phases = []
     for k in range(e2e_steps + 1):
         torch.cuda.synchronize(dev)
