@@ -36,17 +36,20 @@ const char* const kVersion = "v3.3-gb300";
 const char* const kExt[2] = {".dat", ".txt"};
 
 // CRC-32 (IEEE 802.3 polynomial, reflected), as gzip's trailer uses.
-uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
-  static uint32_t table[256];
-  static bool init = false;
-  if (!init) {
+struct Crc32Table {
+  uint32_t v[256];
+  Crc32Table() {
     for (uint32_t i = 0; i < 256; ++i) {
       uint32_t c = i;
       for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-      table[i] = c;
+      v[i] = c;
     }
-    init = true;
   }
+};
+
+uint32_t crc32_update(uint32_t crc, const unsigned char* p, size_t n) {
+  static const Crc32Table tab;  // built once, thread-safe (a function-local static)
+  const uint32_t* table = tab.v;
   crc = ~crc;
   for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
   return ~crc;
