@@ -1913,15 +1913,17 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
               const float4 v = fs.pt[k];
               const float dx = v.x - q.tx, dy = v.y - q.ty, dz = v.z - q.tz;
               const float d = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-              if (d < second && v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz &&
-                  v.z < q.hiz) {
-                if (d < best) {
-                  second = best;
-                  best = d;
-                  bpos = fs.pp[k];
-                  borig = __float_as_int(v.w);
-                } else {
-                  second = d;
+              // rare once the lane has two in-box points: kept a branch around the box test
+              if (__builtin_expect(d < second, 0)) {
+                if (v.x > q.lox && v.x < q.hix && v.y > q.loy && v.y < q.hiy && v.z > q.loz && v.z < q.hiz) {
+                  if (d < best) {
+                    second = best;
+                    best = d;
+                    bpos = fs.pp[k];
+                    borig = __float_as_int(v.w);
+                  } else {
+                    second = d;
+                  }
                 }
               }
             }
