@@ -16,6 +16,7 @@
 // returns the same bytes as the uncompressed file.
 #include <algorithm>
 #include <charconv>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <iterator>
@@ -209,6 +210,79 @@ void GoftCube::writegoftcube(const std::string filename) {
   }
 }
 
+// The values of a text cube's body: `count` whitespace-separated numbers, value
+// t into cols[t % ncol][t / ncol].  The stream reads each with strtof in the
+// "C" locale (correctly rounded); std::from_chars is correctly rounded too, so
+// a token it takes whole, as a finite float, gives the stream's value.  The
+// tokens are parsed by several threads, each on a stretch of whole tokens.
+// False when any token is not of that plain form (a sign '+', a value out of
+// the float range, text): the caller then reads the body through the stream,
+// with the stream's own rules for such tokens.
+static bool parse_text_values(const std::string& body, size_t count, const std::vector<float*>& cols) {
+  const size_t ncol = cols.size();
+  const char* const b = body.data();
+  const size_t len = body.size();
+  auto space = [](char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; };
+  const int nthreads = (int)std::max(
+      1u, std::min({std::thread::hardware_concurrency(), 16u, (unsigned)std::max<size_t>(1, len >> 20)}));
+  // stretch k: [cut[k], cut[k+1]), cut at the end of the token the even split falls in
+  std::vector<size_t> cut(nthreads + 1, len);
+  cut[0] = 0;
+  for (int k = 1; k < nthreads; ++k) {
+    size_t p = std::max(cut[k - 1], len / nthreads * k);
+    while (p < len && !space(b[p])) ++p;
+    cut[k] = p;
+  }
+  std::vector<size_t> ntok(nthreads, 0);
+  std::vector<char> ok(nthreads, 1);
+  auto run = [&](auto&& fn) {
+    std::vector<std::thread> pool;
+    int t = 1;
+    try {
+      for (; t < nthreads; ++t) pool.emplace_back(fn, t);
+    } catch (const std::system_error&) {
+      // no thread to be had: this one takes the stretches left
+    }
+    for (int u = t; u < nthreads; ++u) fn(u);
+    fn(0);
+    for (std::thread& th : pool) th.join();
+  };
+  // pass 1: tokens per stretch
+  run([&](int k) {
+    size_t n = 0;
+    for (size_t p = cut[k]; p < cut[k + 1];) {
+      while (p < cut[k + 1] && space(b[p])) ++p;
+      if (p == cut[k + 1]) break;
+      ++n;
+      while (p < cut[k + 1] && !space(b[p])) ++p;
+    }
+    ntok[k] = n;
+  });
+  std::vector<size_t> first(nthreads, 0);
+  for (int k = 1; k < nthreads; ++k) first[k] = first[k - 1] + ntok[k - 1];
+  if (first[nthreads - 1] + ntok[nthreads - 1] < count) return false;  // too few values: the stream's error
+  // pass 2: the values, as far as `count`
+  run([&](int k) {
+    size_t t = first[k];
+    for (size_t p = cut[k]; p < cut[k + 1] && t < count;) {
+      while (p < cut[k + 1] && space(b[p])) ++p;
+      if (p == cut[k + 1]) break;
+      size_t q = p;
+      while (q < cut[k + 1] && !space(b[q])) ++q;
+      float v = 0.0f;
+      const std::from_chars_result r = std::from_chars(b + p, b + q, v, std::chars_format::general);
+      if (r.ec != std::errc() || r.ptr != b + q || !std::isfinite(v)) {
+        ok[k] = 0;
+        return;
+      }
+      cols[t % ncol][t / ncol] = v;
+      ++t;
+      p = q;
+    }
+  });
+  return std::all_of(ok.begin(), ok.end(), [](char c) { return c != 0; });
+}
+
 // Reads a cube written by writegoftcube: the binary (.dat) or text (.txt)
 // format above, or the header-less text format of FoMo before 3.4 (dim, ng,
 // nvars, table, abundance file, then the values).  lambda0 is taken from the
@@ -276,11 +350,26 @@ void GoftCube::readgoftcube(const std::string emissionsave) {
     }
     rgrid.assign(rdim, tcoord(rng));
     rvars.assign(rnvars, tphysvar(rng));
-    for (int j = 0; j < rng; ++j) {
-      for (int i = 0; i < rdim; ++i) in >> rgrid[i][j];
-      for (int i = 0; i < rnvars; ++i) in >> rvars[i][j];
+    std::vector<float*> cols;
+    for (int i = 0; i < rdim; ++i) cols.push_back(rgrid[i].data());
+    for (int i = 0; i < rnvars; ++i) cols.push_back(rvars[i].data());
+    // the rest of the file, in one read
+    const std::streampos here = in.tellg();
+    in.seekg(0, std::ios::end);
+    const std::streamoff rest = in.tellg() - here;
+    in.seekg(here);
+    std::string body((size_t)std::max<std::streamoff>(rest, 0), '\0');
+    in.read(&body[0], (std::streamsize)body.size());
+    body.resize((size_t)in.gcount());
+    if (!parse_text_values(body, (size_t)rng * cols.size(), cols)) {
+      // value by value through the stream, as the reference reads them
+      std::istringstream bs(body);
+      for (int j = 0; j < rng; ++j) {
+        for (int i = 0; i < rdim; ++i) bs >> rgrid[i][j];
+        for (int i = 0; i < rnvars; ++i) bs >> rvars[i][j];
+      }
+      if (!bs) throw std::runtime_error("FoMo: truncated cube file " + emissionsave);
     }
-    if (!in) throw std::runtime_error("FoMo: truncated cube file " + emissionsave);
   }
   dim = (unsigned int)rdim;
   ng = (unsigned int)rng;

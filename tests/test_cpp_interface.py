@@ -187,6 +187,59 @@ def test_text_writer_formats_every_float_like_the_stream(programs, tmp_path):
         assert printf_g8(v) == "%.8g" % v
 
 
+def test_text_reader_reads_what_the_stream_reads(programs, tmp_path):
+    """readgoftcube parses a text body by several threads with std::from_chars;
+    every value must be the float the reference's stream read (strtof in the
+    "C" locale) gives.  The same file with its first value written "+v" (a
+    form only the stream takes) is read value by value through the stream: the
+    two reads must agree bit for bit, and with the C library's strtof on a
+    sample.  Text the stream rejects (nan, a missing value) is an error."""
+    import ctypes
+    rng = np.random.default_rng(5)
+    ng = 9 * 32768 + 77
+    bits = rng.integers(0, 2 ** 32, ng, dtype=np.uint64).astype(np.uint32)
+    bits[(bits & 0x7F800000) == 0x7F800000] &= 0xBF7FFFFF  # finite only: the stream reads no inf or nan
+    bits[0] &= 0x7FFFFFFF  # the first value positive, so that "+v" is a number
+    cols = np.stack([bits.view(np.float32),
+                     (rng.standard_normal(ng) * 10.0 ** rng.integers(-30, 30, ng)).astype(np.float32),
+                     np.arange(ng, dtype=np.float32)])
+    src = str(tmp_path / "in.dat")
+    _write_dat(src, cols, 2, ["Mm", "Mm", "erg"])
+    txt = str(tmp_path / "in.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, txt, "2"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    raw = open(txt, "rb").read()
+    lines = raw.split(b"\n")
+    plus = str(tmp_path / "plus.txt")
+    lines_p = list(lines)
+    lines_p[7] = b"+" + lines_p[7]
+    open(plus, "wb").write(b"\n".join(lines_p))
+    got = {}
+    for name, path in (("fast", txt), ("stream", plus)):
+        out = str(tmp_path / (name + ".dat"))
+        r = subprocess.run([programs["roundtrip_cube"], path, out, "1"], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        got[name] = read_cube(out)["data"]
+    assert got["fast"].shape == (ng, 3)
+    assert np.array_equal(got["fast"].view(np.uint32), got["stream"].view(np.uint32))
+    assert np.array_equal(got["fast"][:, 2], np.arange(ng, dtype=np.float32))  # every value in its place
+    libc = ctypes.CDLL(None)
+    libc.strtof.restype = ctypes.c_float
+    libc.strtof.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+    for j in rng.choice(ng, 3000, replace=False):
+        toks = lines[7 + j].split()
+        for c in range(2):
+            want = np.float32(libc.strtof(toks[c], None))
+            assert got["fast"][j, c].view(np.uint32) == want.view(np.uint32), (j, c, toks[c])
+    # what the stream cannot read is an error, as in the reference
+    for k, bad in enumerate((lines[:7] + [b"nan 1 2 "] + lines[8:], lines[:-3] + [b""])):
+        path = str(tmp_path / f"bad{k}.txt")
+        open(path, "wb").write(b"\n".join(bad))
+        r = subprocess.run([programs["roundtrip_cube"], path, str(tmp_path / "bad.dat"), "1"],
+                           capture_output=True, text=True)
+        assert r.returncode == 2 and "truncated cube file" in r.stderr, (k, r.stderr)
+
+
 def _write_data(path, snap):
     cols = np.stack([snap.x, snap.y, snap.z, snap.n, snap.T, snap.vx, snap.vy, snap.vz], axis=1)
     with open(path, "w") as f:
