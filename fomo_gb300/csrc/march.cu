@@ -1743,7 +1743,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasSplit) march_split(MarchArgs
 // equator): each one's own ring walk would scan every cell of the lens where
 // the ball of its neighbour's distance cuts into the cloud, and consecutive
 // samples scan almost the same lens.  Here each pending sample gets a ball --
-// at first its distance to the points' bounding box plus two cells -- and
+// at first its distance to the points' bounding box plus three cells -- and
 // each lane marks, in shared memory, the x range its ball covers in every row
 // of cells it reaches; the warp then gathers those rows (the union of the
 // balls), testing each gathered point against every sample's box as the
@@ -1796,7 +1796,7 @@ __device__ __forceinline__ unsigned far_half(const SnapDev& S, const BoxQ& q, bo
   const float dyg = fmaxf(fmaxf(g.miny - q.ty, q.ty - g.maxy), 0.0f);
   const float dzg = fmaxf(fmaxf(g.minz - q.tz, q.tz - g.maxz), 0.0f);
   const float L2 = fmaf(dzg, dzg, fmaf(dyg, dyg, dxg * dxg));
-  float margin2 = 4.0f * h * h;  // the ball's margin beyond that bound, squared: two cells at first
+  float margin2 = 9.0f * h * h;  // the ball's margin beyond that bound, squared: three cells at first
   float r2 = L2 + margin2;
   // far samples only (half a cell or more off the points): near and inside the
   // cloud the balls' union holds too many points for every lane to test
