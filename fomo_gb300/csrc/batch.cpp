@@ -51,6 +51,7 @@ extern "C" {
 
 int fomo_render_batch_graph(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_outs, void* stream) {
   if (!ctx || !reqs || nreq <= 0 || !d_outs) return FOMO_EINVAL;
+  NvtxRange range("fomo: render batch (graph)");
   cudaSetDevice(ctx->device);
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   Plan plan;
@@ -101,6 +102,7 @@ int fomo_render_batch_graph(fomo_ctx* ctx, const fomo_request* reqs, int nreq, f
 // "<class> tile_w tile_h blocks_per_sm rscale ms".
 int fomo_autotune(fomo_ctx* ctx, const fomo_request* reqs, int nreq, const char* cache_path) {
   if (!ctx || !reqs || nreq <= 0) return FOMO_EINVAL;
+  NvtxRange range("fomo: autotune");
   cudaSetDevice(ctx->device);
   std::vector<size_t> off(nreq);
   size_t total = 0;

@@ -287,6 +287,7 @@ GridParams choose_grid(const float* mn, const float* mx, int64_t n, double ppc) 
 constexpr double kUniformEmpty = 0.10;  // empty-cell share below which a cloud counts as uniform
 
 int build_snapshot(fomo_ctx* ctx, int64_t n, const float* const host[8], SnapRec* out) {
+  NvtxRange range("fomo: snapshot upload and index");
   cudaStream_t s = ctx->stream;
   // staging: 8 arrays of n floats (z may be absent -> zeros, as nn:82 for 2-D data)
   float* stage = nullptr;
@@ -454,6 +455,7 @@ SnapDev snap_dev(const SnapRec& r) {
 // computed once and kept resident (the reference recomputes it on every
 // render, fomo-object.cpp:389-400).
 int get_payload(fomo_ctx* ctx, int snap, int table, int imaging, double abund, const float2** out) {
+  NvtxRange range("fomo: emissivity");
   auto key = std::make_tuple(snap, table, imaging, abund);
   auto it = ctx->payloads.find(key);
   if (it != ctx->payloads.end()) {
@@ -697,6 +699,7 @@ std::string workload_class(const PlanGroup& G, const SnapRec& snap) {
 // the scratch arena of `scr`, so a plan can be captured in a CUDA graph.
 int plan_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* d_out, int32_t* const* d_nn,
                ScratchSet* scr, Plan* plan) {
+  NvtxRange range("fomo: plan");
   plan->groups.clear();
   plan->view_of_req.assign(nreq, -1);
   plan->nviews_total = 0;
@@ -957,6 +960,7 @@ static std::vector<int> view_ranges(const PlanGroup& G, bool split, double range
 
 int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s, const RangeDone* done,
                double range_cost) {
+  NvtxRange range("fomo: launch");
   char* db = scr->arena.base;
   // Under stream capture an ordinary event record is only a capture-internal
   // dependency: the staging event is then recorded after the graph launch,
@@ -1421,6 +1425,7 @@ int fomo_render_device(fomo_ctx* ctx, const fomo_request* req, float* d_out_cube
 
 int fomo_render_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* const* outs, fomo_view_info* infos) {
   if (!ctx || !reqs || nreq <= 0 || !outs) return FOMO_EINVAL;
+  NvtxRange range("fomo: render batch to host");
   cudaSetDevice(ctx->device);
   for (int r = 0; r < nreq; ++r) {
     int rc = validate(ctx, reqs[r]);
@@ -1490,6 +1495,7 @@ int fomo_render_batch(fomo_ctx* ctx, const fomo_request* reqs, int nreq, float* 
 
 int fomo_render(fomo_ctx* ctx, const fomo_request* req, float* out_cube, int32_t* out_nn_idx, fomo_view_info* info) {
   if (!ctx || !req || !out_cube) return FOMO_EINVAL;
+  NvtxRange range("fomo: render to host");
   cudaSetDevice(ctx->device);
   int rc = validate(ctx, *req);
   if (rc) return rc;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <functional>
 #include <map>
@@ -13,6 +14,18 @@
 #include "fomo_internal.h"
 
 namespace fomo {
+
+// A named range of the host thread on the NVTX timeline (Nsight Systems, ncu
+// --nvtx) around one stage of the library: snapshot upload and index build,
+// emissivity, batch planning and launch, downloads, autotuning, a server
+// batch.  Header-only NVTX 3: without a tool attached a range costs a few
+// nanoseconds.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct TableHost {
   std::string ion, unit;

@@ -155,6 +155,7 @@ void finish_slot(fomo_server* S, Slot& sl, int status) {
 // Launch the admitted requests `ids` on slot `sl`; called without S->mu held.
 int launch_slot(fomo_server* S, Slot& sl, std::vector<uint64_t>& ids, std::vector<fomo_request>& reqs,
                 std::vector<size_t>& out_bytes) {
+  NvtxRange range("fomo server: launch a batch");
   fomo_ctx* ctx = S->ctx;
   const int n = (int)reqs.size();
   std::vector<size_t> doff(n), hoff(n);
