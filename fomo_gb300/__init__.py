@@ -37,9 +37,10 @@ COUNTERS = ("segments", "candidates", "rows", "points_loaded", "not_gathered", "
 
 
 class FomoError(RuntimeError):
-    def __init__(self, code: int, msg: str):
+    def __init__(self, code: int, msg: str, stats=None):
         super().__init__(f"[{code}] {msg}")
         self.code = code
+        self.stats = stats  # Server.wait: the request's timestamps (RequestStats) when it ended with an error
 
 
 class Request(ctypes.Structure):
@@ -420,7 +421,7 @@ class Server:
         if rc != OK:
             if rc != ETIMEOUT:
                 self._outs.pop(ticket, None)
-            raise FomoError(rc, self._L.fomo_server_last_error(self.h).decode())
+            raise FomoError(rc, self._L.fomo_server_last_error(self.h).decode(), None if rc == ETIMEOUT else st)
         self._outs.pop(ticket, None)
         return st
 

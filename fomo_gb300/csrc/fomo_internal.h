@@ -121,6 +121,8 @@ struct MarchArgs {
   const float2* totpol;          // Thomson: sorted (n*totterm, n*polterm)
   float rscale;                  // gather radius of the search in local point spacings (0: the default, 0.9)
   unsigned long long* stats;     // optional search counters (profiling), else null
+  const unsigned* stop;          // a server batch's stop word (device memory), or null: once it is
+                                 // set, the ray-queue kernels take no further rays
 };
 
 // Search counters accumulated when MarchArgs::stats is set.

@@ -247,7 +247,14 @@ __device__ __forceinline__ bool next_ray(const MarchArgs& a, const double3* ktab
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long item = 0;
-    if (lane == 0) item = atomicAdd(a.counter + ctr, 1ull);
+    if (lane == 0) {
+      item = atomicAdd(a.counter + ctr, 1ull);
+      // a stopped batch (every request of it cancelled): the queue counts as
+      // drained.  The word only goes from 0 to 1 while a batch runs, so a
+      // kernel that starts after one that stopped stops at its first ray too
+      // (an emission pass reads no position its search did not write).
+      if (a.stop && __ldcv(a.stop) != 0u) item = (unsigned long long)a.total_items;
+    }
     item = __shfl_sync(kFull, item, 0) + (unsigned long long)a.item_base;
     if ((int64_t)item >= a.total_items) return false;
     if (ray_of_item(a, ktab, ktab_stride, (int64_t)item, r)) return true;

@@ -1008,6 +1008,7 @@ int issue_plan(fomo_ctx* ctx, const Plan& plan, ScratchSet* scr, cudaStream_t s,
     a.totpol = G.totpol;
     a.stats = ctx->march_stats;
     a.rscale = G.rscale;
+    a.stop = scr->stop;
     if (e == cudaSuccess && scr->ev0 && ctx->time_march) e = record_timing(scr->ev0);
     MarchTimer* timer = (ctx->kernel_timing && !capturing) ? &ctx->timer : nullptr;
     int rc = FOMO_OK;

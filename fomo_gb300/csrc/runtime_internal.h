@@ -78,6 +78,7 @@ struct Staging {
 struct ScratchSet {
   Arena arena;
   Staging staging;
+  unsigned* stop = nullptr;  // a server slot's stop word (device), null for the context's own batches
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaError_t init() {
     cudaError_t e = cudaEventCreate(&ev0);

@@ -78,6 +78,13 @@ struct Slot {
   std::deque<std::pair<cudaEvent_t, std::vector<uint64_t>>> ranges;
   bool busy = false;
   double t_launch = 0;
+  // halting a batch whose requests were all cancelled: the march kernels
+  // read halt_dev (ScratchSet::stop) before each ray; a cancellation sets it
+  // with a copy on the server's control stream and records halt_ev after the
+  // copy; the slot's next batch waits for halt_ev and clears the word first
+  unsigned* halt_dev = nullptr;
+  cudaEvent_t halt_ev = nullptr;
+  bool halt_sent = false;
 };
 
 // Work per view range of a slot's batch (LOS samples + output cells): about a
@@ -106,6 +113,8 @@ struct fomo_server {
   int inflight = 0;
   bool stop = false;
   Slot slots[2];
+  cudaStream_t ctrl = nullptr;   // control copies (halt words), beside the slots' streams
+  unsigned* halt_host = nullptr; // pinned {0, 1}: the halt word's two values
   std::string err;
   double t0 = 0;
 };
@@ -179,6 +188,10 @@ int launch_slot(fomo_server* S, Slot& sl, std::vector<uint64_t>& ids, std::vecto
   double largest = 0.0;
   for (const fomo_request& q : reqs) largest = std::max(largest, (double)q.nx * q.ny * q.nz);
   sl.stream = largest <= kServeSmallSamples ? sl.stream_hi : sl.stream_lo;
+  cudaError_t eh = cudaStreamWaitEvent(sl.stream, sl.halt_ev, 0);
+  if (eh == cudaSuccess)
+    eh = cudaMemcpyAsync(sl.halt_dev, S->halt_host, sizeof(unsigned), cudaMemcpyHostToDevice, sl.stream);
+  if (eh != cudaSuccess) return cuda_err(ctx, eh, "halt word");
   Plan plan;
   rc = plan_batch(ctx, reqs.data(), n, d.data(), nullptr, &sl.scr, &plan);
   if (rc) return rc;
@@ -282,6 +295,7 @@ void scheduler(fomo_server* S) {
       if (!ids.empty()) {
         free_slot->busy = true;
         free_slot->ids = ids;
+        free_slot->halt_sent = false;
         lk.unlock();
         int rc = launch_slot(S, *free_slot, ids, reqs, out_bytes);
         if (rc != FOMO_OK) cudaStreamSynchronize(free_slot->stream);  // part of the batch may be queued
@@ -331,6 +345,19 @@ int fomo_server_create(const fomo_server_config* config, fomo_server** out) {
     }
     sl.stream = sl.stream_lo;
   }
+  bool ok = cudaStreamCreateWithFlags(&S->ctrl, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMallocHost(reinterpret_cast<void**>(&S->halt_host), 2 * sizeof(unsigned)) == cudaSuccess;
+  for (Slot& sl : S->slots)
+    ok = ok && cudaMalloc(reinterpret_cast<void**>(&sl.halt_dev), 256) == cudaSuccess &&
+         cudaMemset(sl.halt_dev, 0, sizeof(unsigned)) == cudaSuccess &&
+         cudaEventCreateWithFlags(&sl.halt_ev, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    fomo_server_destroy(S);
+    return FOMO_EDEVICE;
+  }
+  S->halt_host[0] = 0u;
+  S->halt_host[1] = 1u;
+  for (Slot& sl : S->slots) sl.scr.stop = sl.halt_dev;
   S->t0 = now_s();
   S->worker = std::thread(scheduler, S);
   *out = S;
@@ -399,6 +426,26 @@ int fomo_server_cancel(fomo_server* S, uint64_t ticket) {
   auto it = S->tickets.find(ticket);
   if (it == S->tickets.end()) return FOMO_ENOTFOUND;
   it->second.cancelled = true;  // queued: dropped at admission; running: result discarded
+  if (it->second.state == TState::kRunning) {
+    // a batch left with no request to deliver is halted on the device
+    for (Slot& sl : S->slots) {
+      if (!sl.busy || sl.halt_sent || std::find(sl.ids.begin(), sl.ids.end(), ticket) == sl.ids.end()) continue;
+      bool all = true;
+      for (uint64_t id : sl.ids) {
+        auto jt = S->tickets.find(id);
+        if (jt != S->tickets.end() && !jt->second.cancelled && jt->second.state != TState::kDone) all = false;
+      }
+      if (!all) continue;
+      int prev = -1;
+      cudaGetDevice(&prev);  // the caller's thread keeps its current device
+      cudaSetDevice(S->ctx->device);
+      if (cudaMemcpyAsync(sl.halt_dev, S->halt_host + 1, sizeof(unsigned), cudaMemcpyHostToDevice, S->ctrl) ==
+              cudaSuccess &&
+          cudaEventRecord(sl.halt_ev, S->ctrl) == cudaSuccess)
+        sl.halt_sent = true;
+      if (prev >= 0) cudaSetDevice(prev);
+    }
+  }
   S->cv.notify_all();
   return FOMO_OK;
 }
@@ -422,7 +469,14 @@ int fomo_server_destroy(fomo_server* S) {
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream_lo) cudaStreamDestroy(sl.stream_lo);
     if (sl.stream_hi) cudaStreamDestroy(sl.stream_hi);
+    if (sl.halt_ev) cudaEventDestroy(sl.halt_ev);
+    if (sl.halt_dev) cudaFree(sl.halt_dev);
   }
+  if (S->ctrl) {
+    cudaStreamSynchronize(S->ctrl);
+    cudaStreamDestroy(S->ctrl);
+  }
+  if (S->halt_host) cudaFreeHost(S->halt_host);
   fomo_ctx_destroy(S->ctx);
   delete S;
   return FOMO_OK;

@@ -328,6 +328,10 @@ fomo_ctx* fomo_server_context(fomo_server* srv);
  * FOMO_EADMISSION at submit. */
 int fomo_server_submit(fomo_server* srv, const fomo_request* req, float* out_host, uint64_t* ticket);
 int fomo_server_wait(fomo_server* srv, uint64_t ticket, double timeout_s, fomo_request_stats* stats);
+/* Cancel (thread-safe): a queued request is dropped; a running one completes
+ * with FOMO_ECANCELLED and its cube is not delivered.  When every request of
+ * a running batch is cancelled, the batch is halted on the device: its march
+ * kernels take no further rays (a stop word read before each ray). */
 int fomo_server_cancel(fomo_server* srv, uint64_t ticket);
 /* Drain, stop the scheduler thread and free the context. */
 int fomo_server_destroy(fomo_server* srv);

@@ -71,10 +71,17 @@ def test_cancel_queued_request():
 
 
 def test_cancel_running_request():
+    """A running request that is cancelled ends FOMO_ECANCELLED, undelivered;
+    its batch (no other request in it) is halted on the device, so it ends
+    well before the same request rendered in full; the next batch on the
+    same slot renders normally (its halt word cleared)."""
     with fg.Server(0, max_inflight=1) as srv:
         sid, tid = _setup(srv.ctx)
         warm = np.empty(fg.Context.cube_shape(_small(sid, tid)), np.float32)
         srv.wait(srv.submit(_small(sid, tid), warm))
+        full = np.empty(fg.Context.cube_shape(_big(sid, tid)), np.float32)
+        st = srv.wait(srv.submit(_big(sid, tid), full))
+        t_full = st.t_done - st.t_start
         a = np.full(fg.Context.cube_shape(_big(sid, tid)), SENTINEL, np.float32)
         ta = srv.submit(_big(sid, tid), a)
         time.sleep(0.02)  # admitted at once and on the device by now
@@ -83,9 +90,16 @@ def test_cancel_running_request():
             srv.wait(ta)
         assert ei.value.code == fg.ECANCELLED
         assert (a == SENTINEL).all()  # the rendered cube is discarded, not delivered
-        c = np.empty_like(warm)
-        assert srv.wait(srv.submit(_small(sid, tid), c)).status == fg.OK
-        np.testing.assert_array_equal(c, warm)
+        t_cancelled = ei.value.stats.t_done - ei.value.stats.t_start
+        assert t_full > 0.05, t_full  # the full render takes long enough for the comparison
+        assert t_cancelled < 0.6 * t_full, (t_cancelled, t_full)
+        for _ in range(2):  # both slots have run since
+            c = np.empty_like(warm)
+            assert srv.wait(srv.submit(_small(sid, tid), c)).status == fg.OK
+            np.testing.assert_array_equal(c, warm)
+        again = np.empty_like(full)
+        assert srv.wait(srv.submit(_big(sid, tid), again)).status == fg.OK
+        np.testing.assert_array_equal(again, full)
 
 
 def test_stopped_server_drains_its_queue_and_a_new_one_renders_the_same():
