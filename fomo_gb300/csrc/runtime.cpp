@@ -91,22 +91,56 @@ int dev_alloc(fomo_ctx* ctx, void** p, size_t bytes) {
       << ctx->budget << " used)";
     return set_err(ctx, FOMO_ENOMEM, m.str());
   }
-  cudaError_t e = cudaMalloc(p, bytes);
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    return cuda_err(ctx, e, "cudaMalloc");
+  // a block of this size freed before (a snapshot, table or emissivity made
+  // again for the same number of points) is used again as it is
+  auto fb = ctx->free_blocks.find(bytes);
+  if (fb != ctx->free_blocks.end()) {
+    *p = fb->second;
+    ctx->free_blocks.erase(fb);
+    ctx->cached -= bytes;
+  } else {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && !ctx->free_blocks.empty()) {
+      cudaGetLastError();  // clear the sticky-free error state, give the kept blocks back and try again
+      release_free_blocks(ctx);
+      e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess) {
+      *p = nullptr;
+      return cuda_err(ctx, e, "cudaMalloc");
+    }
   }
   ctx->used += bytes;
   ctx->sizes[*p] = bytes;
   return FOMO_OK;
 }
 
+// Blocks kept by dev_free: at most kKeepBlock bytes each and kKeepTotal in all.
+constexpr size_t kKeepBlock = size_t(512) << 20;
+constexpr size_t kKeepTotal = size_t(4) << 30;
+
+void release_free_blocks(fomo_ctx* ctx) {
+  for (auto& kv : ctx->free_blocks) cudaFree(kv.second);
+  ctx->free_blocks.clear();
+  ctx->cached = 0;
+}
+
 void dev_free(fomo_ctx* ctx, void* p) {
   if (!p) return;
   auto it = ctx->sizes.find(p);
+  size_t bytes = 0;
   if (it != ctx->sizes.end()) {
-    ctx->used -= it->second;
+    bytes = it->second;
+    ctx->used -= bytes;
     ctx->sizes.erase(it);
+  }
+  if (bytes > 0 && bytes <= kKeepBlock && ctx->cached + bytes <= kKeepTotal) {
+    // kept for the next allocation of the same size instead of unmapped and
+    // mapped again; like cudaFree, only once the device is done with it
+    cudaDeviceSynchronize();
+    ctx->free_blocks.emplace(bytes, p);
+    ctx->cached += bytes;
+    return;
   }
   cudaFree(p);
 }
@@ -1182,6 +1216,7 @@ int fomo_ctx_destroy(fomo_ctx* ctx) {
   for (auto& kv : ctx->tables) dev_free(ctx, kv.second.d);
   dev_free(ctx, ctx->scratch.arena.base);
   dev_free(ctx, ctx->out_arena.base);
+  release_free_blocks(ctx);
   if (ctx->stats_dev) cudaFree(ctx->stats_dev);
   if (ctx->timer.ev) {
     for (int i = 0; i < ctx->timer.cap; ++i) cudaEventDestroy(ctx->timer.ev[i]);

@@ -161,6 +161,9 @@ struct fomo_ctx {
   size_t budget = 0;
   size_t used = 0;
   std::map<void*, size_t> sizes;
+  // freed blocks kept for an allocation of the same size (dev_free / dev_alloc)
+  std::multimap<size_t, void*> free_blocks;
+  size_t cached = 0;
   int next_id = 1;
   std::string err;
   std::map<int, fomo::SnapRec> snaps;
@@ -199,6 +202,7 @@ int set_err(fomo_ctx* c, int code, const std::string& msg);
 int cuda_err(fomo_ctx* c, cudaError_t e, const char* what);
 int dev_alloc(fomo_ctx* ctx, void** p, size_t bytes);
 void dev_free(fomo_ctx* ctx, void* p);
+void release_free_blocks(fomo_ctx* ctx);  // cudaFree of the blocks dev_free kept
 int validate(fomo_ctx* ctx, const fomo_request& q);
 size_t cube_elems(const fomo_request& q);
 // Called by issue_plan once the work of views [v0, v1) of launch G is on the
