@@ -124,6 +124,30 @@ def test_gzip_option_and_delete_option(programs, tmp_path):
     assert read_cube(str(tmp_path / "d.dat.gz"))["body"] == read_cube(src)["body"]
 
 
+def test_gzip_output_is_compressed_and_exact(programs, tmp_path):
+    """The .gz files are DEFLATE streams (several 1 MB chunks compressed at
+    once, Huffman codes made per chunk, stored blocks where the data do not
+    compress) that any gzip reader turns back into the plain file's bytes; the
+    text of a cube compresses as zlib's default level does, within 10 %."""
+    import zlib
+    rng = np.random.default_rng(13)
+    ng = 120_000  # about 5 MB of text: several chunks
+    cols = np.stack([rng.uniform(-5, 5, ng).astype(np.float32), rng.uniform(-5, 5, ng).astype(np.float32),
+                     rng.uniform(170, 172, ng).astype(np.float32),
+                     rng.integers(0, 2 ** 32, ng, dtype=np.uint64).astype(np.uint32).view(np.float32)])
+    src = str(tmp_path / "in.dat")
+    _write_dat(src, cols, 3, ["Mm", "Mm", "A", "erg"])
+    out = str(tmp_path / "z.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, str(0b0111)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for ext in (".txt", ".dat"):
+        plain = open(str(tmp_path / ("z" + ext)), "rb").read()
+        packed = open(str(tmp_path / ("z" + ext + ".gz")), "rb").read()
+        assert gzip.decompress(packed) == plain, ext
+        assert len(packed) <= 1.1 * len(zlib.compress(plain, 6)) + 64, (ext, len(packed), len(plain))
+    assert len(open(str(tmp_path / "z.txt.gz"), "rb").read()) < 0.6 * os.path.getsize(str(tmp_path / "z.txt"))
+
+
 def _write_dat(path, cols, dim, units):
     """A .dat cube (the binary format above) from FP32 columns [dim + nvars][ng]."""
     with open(path, "wb") as f:
