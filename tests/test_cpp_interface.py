@@ -148,6 +148,35 @@ def test_gzip_output_is_compressed_and_exact(programs, tmp_path):
     assert len(open(str(tmp_path / "z.txt.gz"), "rb").read()) < 0.6 * os.path.getsize(str(tmp_path / "z.txt"))
 
 
+def test_gzip_of_skewed_and_repetitive_bytes(programs, tmp_path):
+    """Byte counts in a Fibonacci progression (a Huffman tree 24 deep, which
+    the 15-bit limit of DEFLATE must flatten), long runs (matches of the
+    longest length, 258, at distance 1) and the cube text around them: every
+    .gz must read back to the plain bytes."""
+    rng = np.random.default_rng(17)
+    fib = [1, 1]
+    while len(fib) < 26:
+        fib.append(fib[-1] + fib[-2])
+    skewed = np.repeat(np.arange(26, dtype=np.uint8) * 9 + 7, fib)
+    rng.shuffle(skewed)
+    runs = np.concatenate([np.full(300_000, 0x41, np.uint8), np.full(70_001, 0x00, np.uint8),
+                           np.tile(np.arange(7, dtype=np.uint8), 40_000)])
+    raw = np.concatenate([skewed, runs])
+    raw = raw[: raw.size // 4 * 4]
+    col = raw.view(np.float32)
+    ng = col.size // 2
+    cols = np.stack([col[:ng], col[ng:2 * ng]])
+    src = str(tmp_path / "in.dat")
+    _write_dat(src, cols, 1, ["Mm", "erg"])
+    out = str(tmp_path / "z.txt")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, str(0b0111)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for ext in (".txt", ".dat"):
+        plain = open(str(tmp_path / ("z" + ext)), "rb").read()
+        assert gzip.decompress(open(str(tmp_path / ("z" + ext + ".gz")), "rb").read()) == plain, ext
+    assert os.path.getsize(str(tmp_path / "z.dat.gz")) < 0.7 * os.path.getsize(str(tmp_path / "z.dat"))
+
+
 def _write_dat(path, cols, dim, units):
     """A .dat cube (the binary format above) from FP32 columns [dim + nvars][ng]."""
     with open(path, "wb") as f:
