@@ -580,9 +580,10 @@ def run_ours(args):
             "clocks": clocks,
             "ceilings": ceilings,
             "kernels": kernels,
-            # per step: view init, view extents, view finalize, search, emission, overflow split, deferred march,
-            # hard-sample march
-            "gpu_launches": 8 * args.steps,
+            # per step: view init, view bounds (per block of cells), view extents (the blocks that can hold an
+            # extreme), view finalize, search, overflow split, far pass, deferred march, hard-sample march,
+            # emission
+            "gpu_launches": 10 * args.steps,
             "serving": serving,
         }
         print(json.dumps(out))
