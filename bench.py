@@ -571,7 +571,8 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                          "bytes_per_sample": bps,
                          "kernel": "march_search (neighbour search, positions to a buffer) + march_split "
-                                   "(overflowing segments) + march_deferred (the samples the search leaves) + "
+                                   "(overflowing segments) + march_far (far samples of wide-box views; an empty "
+                                   "list here) + march_deferred (the samples the search leaves) + "
                                    "march_hard (deferred samples over the one-lane budget) + "
                                    "march_spectral<4,1,shade> (emission from the positions), timed together",
                          "binding": binding_bound(kernels)},
