@@ -177,6 +177,24 @@ def test_gzip_of_skewed_and_repetitive_bytes(programs, tmp_path):
     assert os.path.getsize(str(tmp_path / "z.dat.gz")) < 0.7 * os.path.getsize(str(tmp_path / "z.dat"))
 
 
+@pytest.mark.parametrize("ng", [131061, 131062, 131063, 262124])
+def test_gzip_at_chunk_boundaries(programs, tmp_path, ng):
+    """The .dat of a 1-column cube is 80 header bytes + 8 per point: these
+    sizes put its end just before, on and just past the 1 MB chunk boundary
+    of the compressor (a last chunk of 8 bytes), and on two chunks exactly."""
+    rng = np.random.default_rng(ng)
+    cols = np.stack([np.round(rng.uniform(-5, 5, ng), 2).astype(np.float32),
+                     rng.integers(0, 2 ** 32, ng, dtype=np.uint64).astype(np.uint32).view(np.float32)])
+    src = str(tmp_path / "in.dat")
+    _write_dat(src, cols, 1, ["Mm", "erg"])
+    out = str(tmp_path / "z.dat")
+    r = subprocess.run([programs["roundtrip_cube"], src, out, str(0b0101)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    plain = open(out, "rb").read()
+    assert len(plain) == 80 + 8 * ng
+    assert gzip.decompress(open(out + ".gz", "rb").read()) == plain
+
+
 def _write_dat(path, cols, dim, units):
     """A .dat cube (the binary format above) from FP32 columns [dim + nvars][ng]."""
     with open(path, "wb") as f:
